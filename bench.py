@@ -1,0 +1,355 @@
+"""Benchmark of the SEM acoustic step (plain form) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c2|c1] [--kernel auto|element|stencil]
+
+Metric: Gnode-steps/s (global nodes x time steps / second), FP32 fields.  Default workload: the
+at-scale plain configuration, 200^3 hexahedra of 10 m, GLL order 4 (513,922,401 nodes), layered
++ perturbed velocity, 20-element sponge, one Ricker source, 1024 receivers (synthetic inputs,
+seeded).  A "step" is one leapfrog step of the whole mesh.  Fields are 2 GB each, far larger than
+L2, so no L2 flush is needed between steps.
+
+Rank 0 prints one JSON line.  Under torchrun (N > 1) every rank runs an independent replica of
+the workload (the plain step does not shard in this build) and `value` is the sum over ranks of
+node-steps divided by the slowest rank's time.
+
+--impl reference times the reference's CPU implementation of the same step on this machine's
+host cores: the oracle's C restatement (oracle/sem_oracle.c, bit-exact with the compiled
+reference where the reference is available), OpenMP over all cores with race-free element
+colouring, on a bounded sub-box of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "proxy-geos-hc_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "SEM Gnode-steps/s on 1 GB300 (Q4, fp32)"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in self.rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_workload(name: str):
+    from semgb import workloads as W
+    if name == "c2":
+        return W.c2_plain_scale(200, steps=1000)
+    if name == "c1":
+        return W.c1_plain_small(1500)
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU side (oracle restatement of the reference's step)
+# ---------------------------------------------------------------------------------------------
+
+def cpu_sample(wl, n_elems_axis: int):
+    """A bounded sub-box of the workload for the CPU timing: same order, element size and
+    velocity recipe (the box's first elements along each axis), same source/sponge rules."""
+    from semgb import workloads as W
+    import copy
+    s = copy.deepcopy(wl)
+    n = n_elems_axis
+    v = wl.vel.reshape(wl.ey, wl.ez, wl.ex)[:n, :n, :n]
+    s.ex = s.ey = s.ez = n
+    s.vel = np.ascontiguousarray(v.reshape(-1))
+    s.src_xyz = np.array([[n * wl.h / 2, n * wl.h / 2, min(100.0, n * wl.h / 2)]], np.float32)
+    s.rec_xyz = wl.rec_xyz[:16] * (n / wl.ex)
+    s.sponge_thickness = min(wl.sponge_thickness, max(1, n // 4))
+    s.name = f"{wl.name}_cpu_sample_{n}c"
+    return s
+
+
+def time_cpu(wl, steps: int, threads: int):
+    from oracle import oracle as O
+    P = O.problem_from_workload(wl, steps)
+    t0 = time.perf_counter()
+    O.run(P, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return P.n_nodes * steps / dt, dt, P.n_nodes
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    wl = make_workload(args.workload)
+    n = args.ref_elems
+    sw = cpu_sample(wl, n)
+    from oracle import oracle as O
+    O.lib()
+    if args.warmup:
+        time_cpu(sw, 1, threads)
+    rate, secs, nodes = time_cpu(sw, args.steps, threads)
+    g = rate / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": g, "unit": "Gnode-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{wl.name} (CPU sample: {n}^3 elements of the same recipe)",
+                   "order": wl.order, "nodes": nodes, "parallelism": f"openmp x{threads}"},
+        "cpu_baseline": {"value": g, "unit": "Gnode-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{n}^3-element sub-box of {wl.name}, {args.steps} steps"},
+        "e2e": {"value": g, "unit": "Gnode-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------------------------
+
+def traffic_per_node(kernel_name: str):
+    """DRAM bytes per node per launch from the committed ncu summary (profiles/), if any."""
+    p = os.path.join(ROOT, "profiles", "dram_bytes_per_node.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)[kernel_name])
+    except Exception:
+        return None
+
+
+# Algorithmic (compulsory) DRAM bytes per node and launch.
+#  stencil (fused pass): read p^n, p^{n-1}, dt^2/M; write p^{n+1}                    = 16 B
+#  element kernel: connectivity (o+1)^3*4/o^3, gather of p^n, y read-modify-write    = see below
+#  update kernel: read p^n, p^{n-1}, y, dt^2/M; write p^{n+1}, y                    = 24 B
+def element_bytes_per_node(order: int) -> float:
+    return 4.0 * (order + 1) ** 3 / order ** 3 + 4.0 + 8.0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import semgb
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    wl = make_workload(args.workload)
+    kernel = {"auto": semgb.KERNEL_AUTO, "element": semgb.KERNEL_ELEMENT,
+              "stencil": semgb.KERNEL_STENCIL}[args.kernel]
+    mesh, s = semgb.solver_from_workload(wl, kernel)
+    stream = torch.cuda.Stream()
+    s.set_stream(stream.cuda_stream)
+    N = mesh.n_nodes
+    W = max(args.warmup, 3)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
+    # warm-up (also builds the graphs and the mass coefficients)
+    s.step(W)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        s.step(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    t_ms = ev0.elapsed_time(ev1)
+    s.synchronize()
+    t_all = torch.tensor([t_ms], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        dist.all_reduce(t_all, op=dist.ReduceOp.MAX)
+    t_max = float(t_all.item())
+    value = N * args.steps * ws / (t_max / 1e3) / 1e9
+
+    # per-kernel device time (CUDA events on the solver's stream, un-captured launches)
+    kms = s.time_kernels(max(5, min(20, args.steps)))
+    resolved = "stencil" if kernel in (semgb.KERNEL_AUTO, semgb.KERNEL_STENCIL) else "element"
+    peak, peak_kind = hbm_peak()
+    if resolved == "stencil":
+        bpn, kname, kt = 16.0, "sem_stencil", kms[1]
+        launches_per_step = 2
+    else:
+        bpn, kname, kt = element_bytes_per_node(wl.order), "sem_element", kms[1]
+        launches_per_step = 3
+    achieved = bpn * N / (kt / 1e3) / 1e9
+    tpn = traffic_per_node(kname)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": (tpn * N if tpn else None),
+            "kernel": kname, "bytes_per_node": bpn, "kernel_ms": kt, "peak_kind": peak_kind}
+    extra = {}
+    if resolved == "element":
+        upd_b = 24.0 * N
+        extra["roofline_update"] = {"bound": "hbm", "achieved": upd_b / (kms[2] / 1e3) / 1e9,
+                                    "peak": peak, "unit": "GB/s",
+                                    "frac": upd_b / (kms[2] / 1e3) / 1e9 / peak, "kernel_ms": kms[2]}
+    # whole-step bytes under the two-phase byte model (32.3 B/node at Q4) for comparison
+    o = wl.order
+    model_b = 20.0 + 4.0 * (o + 1) ** 3 / o ** 3 + 32.0 / o ** 3
+    step_ms = t_max / args.steps
+    extra["two_phase_model"] = {"bytes_per_node": model_b,
+                                "equivalent_GBps": model_b * N / (step_ms / 1e3) / 1e9,
+                                "frac": model_b * N / (step_ms / 1e3) / 1e9 / peak}
+
+    # end to end through the public streaming call with host buffers: per step, this step's
+    # wavelet sample goes host->device and the step's receiver samples come back
+    nsrc, nrec = s.nsrc, s.nrec
+    wav_h = torch.empty((1, nsrc), dtype=torch.float32, pin_memory=True)
+    tr_h = torch.empty((1, nrec), dtype=torch.float32, pin_memory=True)
+    wav_np, tr_np = wav_h.numpy(), tr_h.numpy()
+    src_w = semgb.ricker(wl.nsteps, wl.dt, float(wl.f0[0]), wl.ricker_order)
+    s.reset()
+    e2e_steps = min(args.steps, wl.nsteps - 2)
+    for i in range(2):  # warm-up of the streaming path
+        wav_np[0, :] = src_w[i]
+        s.step_host(1, wav_np, tr_np)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        wav_np[0, :] = src_w[(i + 2) % len(src_w)]
+        s.step_host(1, wav_np, tr_np)
+    t_e2e = time.perf_counter() - t0
+    e2e_all = torch.tensor([t_e2e], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        dist.all_reduce(e2e_all, op=dist.ReduceOp.MAX)
+    e2e_val = N * e2e_steps * ws / float(e2e_all.item()) / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sw = cpu_sample(wl, args.cpu_elems)
+        rate, secs, nodes = time_cpu(sw, args.cpu_steps, threads)
+        cpu = {"value": rate / 1e9, "unit": "Gnode-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_elems}^3-element sub-box of {wl.name} ({nodes} nodes), "
+                         f"{args.cpu_steps} steps, {secs:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gnode-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": W, "ms_per_step": t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded layered+perturbed velocity model)",
+            "config": {"workload": wl.name, "elements": [wl.ex, wl.ey, wl.ez], "order": wl.order,
+                       "nodes": N, "kernel": resolved, "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (2 GB per field), no flush"},
+            "roofline": roof,
+            **extra,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": "Gnode-steps/s", "h2d_bytes_per_step": 4 * nsrc,
+                    "d2h_bytes_per_step": 4 * nrec, "steps": e2e_steps},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk.summary(),
+            "kernel_ms": {"source": float(kms[0]), "stiffness": float(kms[1]), "update": float(kms[2])},
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    mesh.close()
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["c2", "c1"], default="c2")
+    ap.add_argument("--kernel", choices=["auto", "element", "stencil"], default="auto")
+    ap.add_argument("--cpu-elems", type=int, default=40, help="cpu_baseline sub-box (elements per axis)")
+    ap.add_argument("--cpu-steps", type=int, default=16, help="cpu_baseline steps")
+    ap.add_argument("--ref-elems", type=int, default=32, help="--impl reference sub-box (elements per axis)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

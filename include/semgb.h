@@ -1,0 +1,204 @@
+/*
+ * semgb.h -- C ABI of the GB300-native spectral-element (SEM) acoustic time step.
+ *
+ * This is the drop-in boundary for the reference's SEM solver path (numpex/proxy-geos-hc,
+ * src/sem): mesh and model setup, the per-step compute, source and receiver I/O.  Each entry
+ * point names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status (SEM_OK or a SEM_ERR_* code); sem_last_error_string()
+ *    gives a thread-local message for the last failure on the calling thread.  No C++ exception
+ *    crosses this boundary.
+ *  - The library owns all device memory.  Buffers passed in or out are host memory owned by the
+ *    caller unless a name says "device".  Functions that return data synchronise the solver's
+ *    stream first; sem_solver_step only enqueues work.
+ *  - A handle is used by one host thread at a time; separate solvers may run on separate streams.
+ *  - Node numbering is the reference's: node = ix + iz*nx + iy*nx*nz with nx = ex*order+1 etc.
+ *    (SEMmesh.cpp:142-231); element e = ix + iz*ex + iy*ex*ez; coordinates are (x, y, z).
+ *  - Sizes and node indices are 64-bit.
+ */
+#ifndef SEMGB_H_
+#define SEMGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    SEM_OK = 0,
+    SEM_ERR_ARG = 1,       /* invalid argument (null pointer, size, order, index out of range) */
+    SEM_ERR_CUDA = 2,      /* a CUDA call failed (message has the CUDA error string) */
+    SEM_ERR_OOM = 3,       /* device or host allocation failed */
+    SEM_ERR_TIMEOUT = 4,   /* a bounded device wait gave up */
+    SEM_ERR_UNSTABLE = 5,  /* non-finite values detected in the wavefield or traces */
+    SEM_ERR_STATE = 6      /* call not valid in the handle's current state */
+};
+
+/* Step kernels (sem_solver_set_kernel). */
+enum {
+    SEM_KERNEL_AUTO = 0,     /* fastest available for the mesh (currently SEM_KERNEL_STENCIL) */
+    SEM_KERNEL_ELEMENT = 1,  /* element gather / sum-factorised K.p / atomic scatter + update */
+    SEM_KERNEL_STENCIL = 2   /* tensor-product assembled operator, one fused pass per step */
+};
+
+/* Pressure levels for sem_solver_get_pressure / sem_solver_set_pressure. */
+enum { SEM_LEVEL_CURRENT = 0, SEM_LEVEL_PREVIOUS = 1 };
+
+typedef struct sem_mesh sem_mesh;
+typedef struct sem_solver sem_solver;
+
+const char *sem_last_error_string(void);
+int sem_version(void); /* major*10000 + minor*100 + patch */
+
+/* ------------------------------------------------------------------------------------------
+ * Host-only utilities (no GPU needed).
+ * ------------------------------------------------------------------------------------------ */
+
+/* GLL points xi[order+1], weights w[order+1] (8-decimal values as tabulated by the reference)
+ * and derivative table dphi[(order+1)^2], dphi[j*(order+1)+i] = phi_j'(xi_i); order 1..5.
+ * Replaces SEMQkGLBasisFunctions::gaussLobattoQuadraturePoints/Weights and
+ * getDerivativeBasisFunction1D (SEMQkGLBasisFunctions.hpp:36-117, 310-324). */
+int sem_gll_tables(int order, double *xi, double *w, double *dphi);
+
+/* Ricker wavelet samples out[i] = r(i*dt), order 0, 1 or 2.
+ * Replaces SolverUtils::computeSourceTerm / evaluateRicker (utils.hpp:11-57). */
+int sem_ricker(int nsamples, float dt, float f0, int order, float *out);
+
+/* Node, element and interior-node counts of an ex*ey*ez box of the given order.
+ * Replaces SEMmesh::getNumberOfNodes/Elements/InteriorNodes (SEMmesh.cpp:28-54). */
+int sem_box_counts(int ex, int ey, int ez, int order, int64_t *n_nodes, int64_t *n_elem,
+                   int64_t *n_interior);
+
+/* Element-to-node map rows for elements [e0, e0+count): conn[(e-e0)*(order+1)^3 + local].
+ * Replaces SEMmesh::globalNodesList (SEMmesh.cpp:205-231). */
+int sem_box_connectivity(int ex, int ey, int ez, int order, int64_t e0, int64_t count,
+                         int64_t *conn);
+
+/* Element containing (x,y,z); an axis outside the box maps to element 0 on that axis.
+ * Replaces SEMmesh::getElementNumberFromPoints (SEMmesh.cpp:266-285). */
+int sem_box_element_from_point(int ex, int ey, int ez, float lx, float ly, float lz, float x,
+                               float y, float z, int64_t *element);
+
+/* Nearest GLL node to (x,y,z) (per axis, ties to the lower index, clamped to the box).
+ * The reference has no receivers; this is the build's snapping rule for receiver positions. */
+int sem_box_nearest_node(int ex, int ey, int ez, float lx, float ly, float lz, int order,
+                         float x, float y, float z, int64_t *node);
+
+/* Sponge factors per axis, sx[nx], sy[ny], sz[nz]: for a node at distance d (in elements) from
+ * the nearer face of its axis, s = exp(-sigma*((thickness-d)/thickness)^2) when d < thickness,
+ * else 1; the node factor is (sx[ix]*sy[iy])*sz[iz].  The reference SEM has no sponge; this is
+ * the Gaussian taper of its FD proxy (FDTDinit.hpp:319-396) scaled to `thickness` elements. */
+int sem_box_sponge_profile(int ex, int ey, int ez, float lx, float ly, float lz, int order,
+                           int thickness, float sigma, float *sx, float *sy, float *sz);
+
+/* ------------------------------------------------------------------------------------------
+ * Mesh and model (device).
+ * ------------------------------------------------------------------------------------------ */
+
+/* Structured box of ex*ey*ez hexahedra of order 1..5 over [0,lx]x[0,ly]x[0,lz].  The element
+ * velocity starts at 1500 m/s as in SEMmesh::getModel.
+ * Replaces SEMmesh::SEMmesh (SEMmesh.cpp:3-26) plus the mesh half of
+ * SEMsolver::computeFEInit / initFEarrays (SEMsolver.cpp:12-17, 144-174). */
+int sem_mesh_create_box(int ex, int ey, int ez, float lx, float ly, float lz, int order,
+                        sem_mesh **out);
+int sem_mesh_destroy(sem_mesh *mesh);
+
+/* n_nodes, n_elem, nodes per element, interior nodes. */
+int sem_mesh_info(const sem_mesh *mesh, int64_t *n_nodes, int64_t *n_elem, int *nodes_per_elem,
+                  int64_t *n_interior);
+
+/* Copy the device-resident element-to-node map back (int32, [n_elem][(order+1)^3]) for
+ * bit-exact checks against SEMmesh::globalNodesList (SEMmesh.cpp:205-231). */
+int sem_mesh_get_connectivity(sem_mesh *mesh, int32_t *conn);
+
+/* Per-element velocity c_e (n_elem floats): replaces SEMmesh::getModel (SEMmesh.cpp:288-312).
+ * The nodal mass is M_i = sum over elements e touching i of w_i^3 |detJ| / c_e^2
+ * (SEMsolver.cpp:74-80). */
+int sem_model_set_element_velocity(sem_mesh *mesh, const float *velocity);
+
+/* Per-node squared slowness m_i (n_nodes floats): M_i = m_i * sum_e w_i^3 |detJ|.  Used by the
+ * gradient with respect to m; replaces the element model for subsequent solver steps. */
+int sem_model_set_node_slowness2(sem_mesh *mesh, const float *m);
+
+/* ------------------------------------------------------------------------------------------
+ * Solver.
+ * ------------------------------------------------------------------------------------------ */
+
+/* Solver over `mesh` with time step dt; both pressure levels start at zero.
+ * Replaces SEMsolver::computeFEInit (SEMsolver.cpp:12-17) and SEMproxy::init_arrays
+ * (SEMproxy.cpp:84-90).  The mesh must outlive the solver. */
+int sem_solver_create(sem_mesh *mesh, float dt, sem_solver **out);
+int sem_solver_destroy(sem_solver *s);
+
+/* Run on a caller-provided cudaStream_t (NULL: the solver's own stream). */
+int sem_solver_set_stream(sem_solver *s, void *cuda_stream);
+
+/* Choose the step kernel (SEM_KERNEL_*). */
+int sem_solver_set_kernel(sem_solver *s, int kernel);
+
+/* Sponge of `thickness` elements with boundary damping sigma (0 thickness: none), or explicit
+ * per-axis factors (see sem_box_sponge_profile).  Applied after each step to both levels. */
+int sem_solver_set_sponge(sem_solver *s, int thickness, float sigma);
+int sem_solver_set_sponge_profile(sem_solver *s, const float *sx, const float *sy,
+                                  const float *sz);
+
+/* Point sources on local node 0 of the given elements, wavelet[n_src][n_samples]; the step n
+ * adds dt^2 c_e^2 wavelet[k][n] to the current level at that node (SEMsolver.cpp:39-43,
+ * SEMproxy.cpp:93-119).  _points locates elements from coordinates like
+ * sem_box_element_from_point. */
+int sem_solver_set_sources(sem_solver *s, int n_src, const int64_t *elements,
+                           const float *wavelet, int n_samples);
+int sem_solver_set_source_points(sem_solver *s, int n_src, const float *xyz,
+                                 const float *wavelet, int n_samples);
+
+/* Receivers: sample the new pressure level at these nodes after every step.  The reference
+ * only prints the source node every 100 steps (SEMsolver.cpp:127-142).  _points snaps
+ * positions with sem_box_nearest_node. */
+int sem_solver_set_receiver_nodes(sem_solver *s, int n_rec, const int64_t *nodes);
+int sem_solver_set_receivers(sem_solver *s, int n_rec, const float *xyz);
+
+/* Enqueue n_steps of SEMsolver::computeOneStep followed by the level swap of SEMproxy::run
+ * (SEMsolver.cpp:21-125, SEMproxy.cpp:45-55), plus sponge and receiver sampling.  The time
+ * loop is replayed from a captured CUDA graph. */
+int sem_solver_step(sem_solver *s, int n_steps);
+
+/* Streaming form of the same loop with host buffers: copies this chunk's wavelet samples
+ * (host [n_steps][n_src], replacing the stored wavelet for these steps) to the device, runs
+ * n_steps, and copies the chunk's receiver samples back (host [n_steps][n_rec]).  Either buffer
+ * may be NULL.  Mirrors SEMproxy::run's per-step computeOneStep + outputPnValues. */
+int sem_solver_step_host(sem_solver *s, int n_steps, const float *wavelet_samples,
+                         float *traces_out);
+
+/* Steps completed so far. */
+int sem_solver_steps_done(const sem_solver *s, int64_t *n);
+
+/* Receiver traces [n_steps_done][n_rec] (host), receiver order as given. */
+int sem_solver_get_traces(sem_solver *s, float *out);
+
+/* Read or overwrite one pressure level (n_nodes floats, reference node numbering).
+ * SEM_LEVEL_PREVIOUS is the sponge-damped previous level that the next step uses, as the
+ * reference holds it after its sponge pass; the device keeps it without the last sponge factor
+ * and applies that factor when the level is read, so writing it divides the factor out (exact
+ * to within one rounding). */
+int sem_solver_get_pressure(sem_solver *s, int level, float *out);
+int sem_solver_set_pressure(sem_solver *s, int level, const float *in);
+
+/* Zero both levels, the traces and the step counter. */
+int sem_solver_reset(sem_solver *s);
+
+/* Wait for the solver's stream; returns SEM_ERR_UNSTABLE if any trace sample is non-finite. */
+int sem_solver_synchronize(sem_solver *s);
+
+/* Average device time per launch (ms) of the step's kernels over n_steps un-captured steps,
+ * measured with CUDA events on the solver's stream: ms[0] source, ms[1] stiffness
+ * (element kernel, or the fused stencil pass), ms[2] update (0 for the fused stencil pass).
+ * Advances the solver by n_steps. */
+int sem_solver_time_kernels(sem_solver *s, int n_steps, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SEMGB_H_ */

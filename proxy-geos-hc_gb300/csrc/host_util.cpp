@@ -1,0 +1,175 @@
+// host_util.cpp -- GLL tables, Ricker wavelet, box indexing and sponge profile (host side).
+#include "host_util.h"
+
+#include <cmath>
+
+namespace semgb {
+
+namespace {
+
+// Legendre P_n and its derivative by the three-term recurrence.
+void legendre(int n, double x, double &p, double &dp)
+{
+    double p0 = 1.0, p1 = x, d0 = 0.0, d1 = 1.0;
+    if (n == 0) { p = 1.0; dp = 0.0; return; }
+    for (int k = 2; k <= n; k++) {
+        const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+        const double d2 = d0 + (2.0 * k - 1.0) * p1;
+        p0 = p1; p1 = p2; d0 = d1; d1 = d2;
+    }
+    p = p1; dp = d1;
+}
+
+}  // namespace
+
+bool gll_tables(int order, Gll &g)
+{
+    if (order < kMinOrder || order > kMaxOrder) return false;
+    const int N = order, n1 = order + 1;
+    g.order = order;
+    g.xi[0] = -1.0;
+    g.xi[N] = 1.0;
+    // interior points: Newton on P_N'(x), with P_N'' from the Legendre equation
+    for (int i = 1; i < N; i++) {
+        double x = -std::cos(M_PI * i / N);
+        for (int it = 0; it < 100; it++) {
+            double p, dp;
+            legendre(N, x, p, dp);
+            const double ddp = (2.0 * x * dp - N * (N + 1.0) * p) / (1.0 - x * x);
+            const double dx = dp / ddp;
+            x -= dx;
+            if (std::fabs(dx) < 1e-17) break;
+        }
+        g.xi[i] = x;
+    }
+    for (int i = 0; i < n1 / 2; i++) {  // exact antisymmetry
+        const double a = 0.5 * (g.xi[N - i] - g.xi[i]);
+        g.xi[i] = -a;
+        g.xi[N - i] = a;
+    }
+    if (n1 % 2) g.xi[N / 2] = 0.0;
+    double PN[kMaxOrder + 1];
+    for (int i = 0; i < n1; i++) {
+        double p, dp;
+        legendre(N, g.xi[i], p, dp);
+        PN[i] = p;
+        // the reference tabulates the weights to 8 decimals (SEMQkGLBasisFunctions.hpp:80-117)
+        g.w[i] = std::nearbyint(2.0 / (N * (N + 1.0) * p * p) * 1e8) / 1e8;
+    }
+    for (int j = 0; j < n1; j++)
+        for (int i = 0; i < n1; i++) {
+            double d;
+            if (i != j) d = PN[i] / (PN[j] * (g.xi[i] - g.xi[j]));
+            else if (i == 0) d = -N * (N + 1.0) / 4.0;
+            else if (i == N) d = N * (N + 1.0) / 4.0;
+            else d = 0.0;
+            g.dphi[j * n1 + i] = d;
+        }
+    return true;
+}
+
+float ricker(float time_n, float f0, int order)
+{
+    // float/double mix of utils.hpp:11-46, kept so the samples match the reference bit for bit
+    const float o_tpeak = (float)(1.0 / f0);
+    float pulse = 0.0f;
+    if ((time_n <= -0.9 * o_tpeak) || (time_n >= 2.9 * o_tpeak)) return pulse;
+    const float pi = (float)M_PI;
+    const float lam = (f0 * pi) * (f0 * pi);
+    const float d = time_n - o_tpeak;
+    switch (order) {
+    case 2: pulse = (float)(2.0 * lam * (2.0 * lam * d * d - 1.0) * std::exp(-lam * d * d)); break;
+    case 1: pulse = (float)(-2.0 * lam * d * std::exp(-lam * d * d)); break;
+    case 0: pulse = -d * std::exp(-2 * lam * d * d); break;
+    default: break;
+    }
+    return pulse;
+}
+
+bool make_box(int ex, int ey, int ez, float lx, float ly, float lz, int order, Box &b)
+{
+    if (ex < 1 || ey < 1 || ez < 1 || order < kMinOrder || order > kMaxOrder) return false;
+    if (!(lx > 0) || !(ly > 0) || !(lz > 0)) return false;
+    b.ex = ex; b.ey = ey; b.ez = ez; b.order = order;
+    b.lx = lx; b.ly = ly; b.lz = lz;
+    b.nx = (int64_t)ex * order + 1;
+    b.ny = (int64_t)ey * order + 1;
+    b.nz = (int64_t)ez * order + 1;
+    b.n_nodes = b.nx * b.ny * b.nz;
+    b.n_elem = (int64_t)ex * ey * ez;
+    b.n_interior = (b.nx - 2) * (b.ny - 2) * (b.nz - 2);
+    b.npe = (order + 1) * (order + 1) * (order + 1);
+    return true;
+}
+
+int64_t box_element_from_point(const Box &b, float x, float y, float z)
+{
+    // element sizes are floats there (SEMmesh.cpp:20-22) and the scan keeps the last match
+    const float hx = (float)(b.lx / (1. * b.ex)), hy = (float)(b.ly / (1. * b.ey)),
+                hz = (float)(b.lz / (1. * b.ez));
+    int eX = 0, eY = 0, eZ = 0;
+    for (int i = 0; i < b.ex; i++)
+        if (x >= i * hx && x < (i + 1) * hx) eX = i;
+    for (int i = 0; i < b.ey; i++)
+        if (y >= i * hy && y < (i + 1) * hy) eY = i;
+    for (int i = 0; i < b.ez; i++)
+        if (z >= i * hz && z < (i + 1) * hz) eZ = i;
+    return eX + (int64_t)eZ * b.ex + (int64_t)eY * b.ex * b.ez;
+}
+
+namespace {
+
+int64_t nearest_on_axis(int ne, double len, int order, const double *xi, double c)
+{
+    const double h = len / ne;
+    if (c <= 0.0) return 0;
+    if (c >= len) return (int64_t)ne * order;
+    int64_t e = (int64_t)std::floor(c / h);
+    if (e >= ne) e = ne - 1;
+    int64_t best = e * order;
+    double bd = INFINITY;
+    for (int l = 0; l <= order; l++) {
+        const double d = std::fabs(e * h + (1.0 + xi[l]) * 0.5 * h - c);
+        if (d < bd) { bd = d; best = e * order + l; }
+    }
+    return best;
+}
+
+void sponge_axis(int ne, double len, int order, const double *xi, int thickness, double sigma,
+                 std::vector<float> &s)
+{
+    const double h = len / ne;
+    const int64_t n = (int64_t)ne * order + 1;
+    s.assign(n, 1.0f);
+    for (int64_t i = 0; i < n; i++) {
+        int64_t e = i / order;
+        int l = (int)(i - e * order);
+        if (e == ne) { e = ne - 1; l = order; }
+        const double c = e * h + (1.0 + xi[l]) * 0.5 * h;
+        const double d = std::fmin(c, len - c) / h;
+        if (thickness > 0 && d < thickness) {
+            const double r = (thickness - d) / thickness;
+            s[i] = (float)std::exp(-sigma * r * r);
+        }
+    }
+}
+
+}  // namespace
+
+int64_t box_nearest_node(const Box &b, const Gll &g, float x, float y, float z)
+{
+    const int64_t ix = nearest_on_axis(b.ex, b.lx, b.order, g.xi, x);
+    const int64_t iy = nearest_on_axis(b.ey, b.ly, b.order, g.xi, y);
+    const int64_t iz = nearest_on_axis(b.ez, b.lz, b.order, g.xi, z);
+    return ix + iz * b.nx + iy * b.nx * b.nz;
+}
+
+void box_sponge_profile(const Box &b, const Gll &g, int thickness, double sigma,
+                        std::vector<float> &sx, std::vector<float> &sy, std::vector<float> &sz)
+{
+    sponge_axis(b.ex, b.lx, b.order, g.xi, thickness, sigma, sx);
+    sponge_axis(b.ey, b.ly, b.order, g.xi, thickness, sigma, sy);
+    sponge_axis(b.ez, b.lz, b.order, g.xi, thickness, sigma, sz);
+}
+
+}  // namespace semgb

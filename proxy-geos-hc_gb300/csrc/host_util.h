@@ -1,0 +1,55 @@
+// host_util.h -- host-side (CPU) pieces of the SEM solver: GLL tables, Ricker wavelet, box-mesh
+// indexing, sponge profile.  Used by the C ABI (api.cu) and exported through it.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace semgb {
+
+constexpr int kMinOrder = 1;
+constexpr int kMaxOrder = 5;
+
+struct Gll {
+    int order = 0;
+    double xi[kMaxOrder + 1];
+    double w[kMaxOrder + 1];                       // 8-decimal values, as the reference tabulates
+    double dphi[(kMaxOrder + 1) * (kMaxOrder + 1)];  // dphi[j*(o+1)+i] = phi_j'(xi_i)
+};
+
+// GLL points (roots of P_N' plus the end points), weights 2/(N(N+1)P_N(xi)^2) rounded to 8
+// decimals, and the Lagrange derivative table at the points.  Returns false for a bad order.
+bool gll_tables(int order, Gll &g);
+
+// Ricker wavelet in the reference's float arithmetic (utils.hpp:11-46).
+float ricker(float t, float f0, int order);
+
+struct Box {
+    int ex = 0, ey = 0, ez = 0, order = 0;
+    float lx = 0, ly = 0, lz = 0;
+    int64_t nx = 0, ny = 0, nz = 0;  // nodes per axis
+    int64_t n_nodes = 0, n_elem = 0, n_interior = 0;
+    int npe = 0;                    // nodes per element
+};
+
+bool make_box(int ex, int ey, int ez, float lx, float ly, float lz, int order, Box &b);
+
+// Reference connectivity of element e, local index l + n(o+1) + m(o+1)^2 (SEMmesh.cpp:205-231).
+inline int64_t box_node(const Box &b, int64_t e, int local)
+{
+    const int o = b.order, o1 = o + 1;
+    const int64_t ix = e % b.ex, iz = (e / b.ex) % b.ez, iy = e / ((int64_t)b.ex * b.ez);
+    const int l = local % o1, n = (local / o1) % o1, m = local / (o1 * o1);
+    return (ix * o + l) + (iz * o + n) * b.nx + (iy * o + m) * b.nx * b.nz;
+}
+
+// SEMmesh::getElementNumberFromPoints semantics (SEMmesh.cpp:266-285).
+int64_t box_element_from_point(const Box &b, float x, float y, float z);
+
+// Nearest GLL node per axis, ties to the lower index, clamped to the box.
+int64_t box_nearest_node(const Box &b, const Gll &g, float x, float y, float z);
+
+// Sponge factors along each axis (see semgb.h).
+void box_sponge_profile(const Box &b, const Gll &g, int thickness, double sigma,
+                        std::vector<float> &sx, std::vector<float> &sy, std::vector<float> &sz);
+
+}  // namespace semgb

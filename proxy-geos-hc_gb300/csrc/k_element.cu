@@ -1,0 +1,191 @@
+// k_element.cu -- element-by-element stiffness product of the SEM step on GB300.
+//
+// Replaces the element loop of SEMsolver::computeOneStep (SEMsolver.cpp:46-82) and its per-element
+// computeMassMatrixAndStiffnessVector (SEMQkGLIntegrals.hpp:206-565).  The reference rebuilds the
+// Jacobian, the mass and a dense (o+1)^3-wide stiffness row per node for every element every step
+// (O(n_pe^2) per element).  Here the mass is precomputed once (launch_mass) and K_e.p is
+// sum-factorised: for each reference direction d,
+//     y_d(i) = sum_l phi_i'(xi_l) * g_d * W(l) * sum_m phi_m'(xi_l) * (p_m - p_l)
+// along the 1-D lines ("pencils") of the element, which is O(n_pe*(o+1)) per element.  The first
+// contraction is written in difference form so that a constant field gives exactly zero (the
+// float-rounded derivative table does not sum exactly to zero per row).
+//
+// CTA shape: kElemTile (32) elements x (o+1)^2 warps.  Lane = element of the tile; warp = pencil.
+// All lanes of a warp work on the same local pencil of different elements, so every coefficient
+// index is warp-uniform and shared-memory accesses are unit-stride in the lane.  Phases:
+//   A  the CTA's 32 connectivity rows (contiguous in HBM) -> shared, coalesced
+//   B  gather p through the rows: each thread loads its x-pencil (registers + shared copy)
+//   C  x-direction contraction in registers
+//   D  z-direction (xi2) pencils from shared, result -> s_y
+//   E  y-direction (xi3) pencils from shared, result overwrites the thread's own pencil in s_p
+//   F  y = yx + yz + yy scattered with red.global.add.f32 through the connectivity
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace semgb {
+
+int coef_table_size(int order) { return 3 * (order + 1) * (order + 1); }
+
+namespace {
+
+template <int O>
+struct ElemCfg {
+    static constexpr int O1 = O + 1, NP = O1 * O1, NPE = O1 * O1 * O1;
+    static constexpr int CS = NPE | 1;  // odd row stride: lanes hit distinct banks
+    static constexpr int THREADS = 32 * NP;
+    static constexpr int MINB = O == 1 ? 8 : O == 2 ? 5 : O == 3 ? 3 : O == 4 ? 2 : 1;
+    static constexpr size_t SMEM = sizeof(int) * kElemTile * CS + sizeof(float) * NPE * kElemTile * 2 +
+                                   sizeof(float) * 3 * NP;
+};
+
+// One direction of the element operator along one pencil: out = D^T (c * (D p)), with the first
+// contraction in difference form.  base = g_d * w_a * w_b of the pencil.
+template <int O>
+__device__ __forceinline__ void pencil_apply(const ElementArgs &a, const float (&p)[O + 1],
+                                             float base, float (&out)[O + 1])
+{
+    float g[O + 1];
+#pragma unroll
+    for (int l = 0; l <= O; l++) {
+        float u = 0.f;
+#pragma unroll
+        for (int m = 0; m <= O; m++)
+            if (m != l) u = fmaf(a.D[l][m], p[m] - p[l], u);
+        g[l] = (base * a.w[l]) * u;
+    }
+#pragma unroll
+    for (int i = 0; i <= O; i++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int l = 0; l <= O; l++) acc = fmaf(a.D[l][i], g[l], acc);
+        out[i] = acc;
+    }
+}
+
+template <int O>
+__global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
+    k_element(const ElementArgs a)
+{
+    using C = ElemCfg<O>;
+    constexpr int O1 = C::O1, NP = C::NP, NPE = C::NPE, CS = C::CS, TE = kElemTile;
+    extern __shared__ __align__(16) unsigned char smem[];
+    int *s_conn = reinterpret_cast<int *>(smem);
+    float *s_p = reinterpret_cast<float *>(s_conn + TE * CS);
+    float *s_y = s_p + NPE * TE;
+    float *s_tab = s_y + NPE * TE;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t e0 = (int64_t)blockIdx.x * TE;
+    const int ne = (int)min((int64_t)TE, a.n_elem - e0);
+
+    // A: coefficient table and connectivity rows
+    for (int q = tid; q < 3 * NP; q += C::THREADS) s_tab[q] = __ldg(a.tab + q);
+    {
+        const int32_t *cg = a.conn + e0 * NPE;
+        const int total = ne * NPE;
+        for (int q = tid; q < total; q += C::THREADS) {
+            const int e = q / NPE;
+            s_conn[e * CS + (q - e * NPE)] = __ldg(cg + q);
+        }
+    }
+    __syncthreads();
+
+    const bool act = lane < ne;
+    // B: gather the thread's x-pencil (local j, k fixed)
+    float px[O1];
+    {
+        const int j = warp % O1, k = warp / O1;
+#pragma unroll
+        for (int i = 0; i < O1; i++) {
+            const int node = i + O1 * j + NP * k;
+            float v = 0.f;
+            if (act) v = __ldg(a.p + s_conn[lane * CS + node]);
+            px[i] = v;
+            s_p[node * TE + lane] = v;
+        }
+    }
+    // C: x-direction in registers
+    float yx[O1];
+    {
+        const int j = warp % O1, k = warp / O1;
+        pencil_apply<O>(a, px, s_tab[0 * NP + j + O1 * k], yx);
+    }
+    __syncthreads();
+    // D: z-direction (local index j varies)
+    {
+        const int i = warp % O1, k = warp / O1;
+        float pz[O1], yz[O1];
+#pragma unroll
+        for (int m = 0; m < O1; m++) pz[m] = s_p[(i + O1 * m + NP * k) * TE + lane];
+        pencil_apply<O>(a, pz, s_tab[1 * NP + i + O1 * k], yz);
+#pragma unroll
+        for (int m = 0; m < O1; m++) s_y[(i + O1 * m + NP * k) * TE + lane] = yz[m];
+    }
+    __syncthreads();
+    // E: y-direction (local index k varies); each thread overwrites only its own pencil of s_p
+    {
+        const int i = warp % O1, j = warp / O1;
+        float py[O1], yy[O1];
+#pragma unroll
+        for (int n = 0; n < O1; n++) py[n] = s_p[(i + O1 * j + NP * n) * TE + lane];
+        pencil_apply<O>(a, py, s_tab[2 * NP + i + O1 * j], yy);
+#pragma unroll
+        for (int n = 0; n < O1; n++) s_p[(i + O1 * j + NP * n) * TE + lane] = yy[n];
+    }
+    __syncthreads();
+    // F: scatter through the connectivity
+    if (act) {
+        const int j = warp % O1, k = warp / O1;
+#pragma unroll
+        for (int i = 0; i < O1; i++) {
+            const int node = i + O1 * j + NP * k;
+            const float v = yx[i] + s_y[node * TE + lane] + s_p[node * TE + lane];
+            atomicAdd(a.y + s_conn[lane * CS + node], v);  // result unused: compiles to RED
+        }
+    }
+}
+
+template <int O>
+cudaError_t launch_element_t(const ElementArgs &a, cudaStream_t s)
+{
+    using C = ElemCfg<O>;
+    if (a.n_elem <= 0) return cudaSuccess;
+    const int64_t grid = (a.n_elem + kElemTile - 1) / kElemTile;
+    if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+    k_element<O><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int O>
+cudaError_t setup_t()
+{
+    return cudaFuncSetAttribute(k_element<O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)ElemCfg<O>::SMEM);
+}
+
+}  // namespace
+
+cudaError_t element_kernel_setup()
+{
+    cudaError_t e;
+    if ((e = setup_t<1>()) != cudaSuccess) return e;
+    if ((e = setup_t<2>()) != cudaSuccess) return e;
+    if ((e = setup_t<3>()) != cudaSuccess) return e;
+    if ((e = setup_t<4>()) != cudaSuccess) return e;
+    return setup_t<5>();
+}
+
+cudaError_t launch_element(int order, const ElementArgs &a, cudaStream_t s)
+{
+    switch (order) {
+    case 1: return launch_element_t<1>(a, s);
+    case 2: return launch_element_t<2>(a, s);
+    case 3: return launch_element_t<3>(a, s);
+    case 4: return launch_element_t<4>(a, s);
+    case 5: return launch_element_t<5>(a, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace semgb

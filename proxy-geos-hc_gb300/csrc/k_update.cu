@@ -1,0 +1,185 @@
+// k_update.cu -- node-wise kernels of the SEM step and its set-up.
+//
+//  k_source   SEMsolver.cpp:39-43    p^n[node0(e_k)] += dt^2 c_e^2 r_k(t_n), sources in order
+//  k_update   SEMsolver.cpp:85-89    p^{n+1} = 2 p^n - p^{n-1} - dt^2 y / M on interior nodes,
+//                                    boundary nodes keep p^{n-1} (homogeneous Dirichlet), then the
+//                                    sponge on both levels, receiver sampling, y reset; one pass
+//  k_connectivity  SEMmesh.cpp:205-231 (on the device, for the element kernel)
+//  k_mass     SEMsolver.cpp:33-36,74-80 assembled once: a_i = dt^2 / M_i
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace semgb {
+
+namespace {
+
+__global__ void k_source(const SourceArgs a)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int n = a.ctr[0];
+    if (n < a.nsamples)
+        for (int k = 0; k < a.nsrc; k++)  // in source order, as the reference's loop
+            a.cur[a.node[k]] += a.coef[k] * a.wavelet[(int64_t)k * a.nsamples + n];
+    a.ctr[1] = n;
+    a.ctr[0] = n + 1;
+}
+
+__device__ __forceinline__ int lower_bound64(const int64_t *v, int n, int64_t key)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (v[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <bool SPONGE>
+__global__ void __launch_bounds__(kUpdateThreads) k_update(const UpdateArgs a)
+{
+    constexpr int V = kUpdateNodesPerThread;
+    const int64_t i0 = ((int64_t)blockIdx.x * kUpdateThreads + threadIdx.x) * V;
+    if (i0 < a.n) {
+        const int64_t nxz = a.nx * a.nz;
+        int64_t iy = i0 / nxz;
+        const int64_t r = i0 - iy * nxz;
+        int64_t iz = r / a.nx;
+        int64_t ix = r - iz * a.nx;
+        // arrays are padded to a multiple of 4 floats, so these vector accesses stay in bounds
+        const float4 c4 = *reinterpret_cast<const float4 *>(a.cur + i0);
+        const float4 q4 = *reinterpret_cast<const float4 *>(a.prev + i0);
+        const float4 y4 = *reinterpret_cast<const float4 *>(a.y + i0);
+        const float4 a4 = __ldg(reinterpret_cast<const float4 *>(a.a + i0));
+        const float cc[V] = {c4.x, c4.y, c4.z, c4.w}, qq[V] = {q4.x, q4.y, q4.z, q4.w};
+        const float yy[V] = {y4.x, y4.y, y4.z, y4.w}, aa[V] = {a4.x, a4.y, a4.z, a4.w};
+        float out[V];
+#pragma unroll
+        for (int t = 0; t < V; t++) {
+            out[t] = 0.f;
+            if (i0 + t < a.n) {
+                float s = 1.f;
+                if (SPONGE) s = __ldg(a.sx + ix) * __ldg(a.sy + iy) * __ldg(a.sz + iz);
+                const float qd = SPONGE ? s * qq[t] : qq[t];
+                const bool interior = ix > 0 && ix < a.nx - 1 && iz > 0 && iz < a.nz - 1 &&
+                                      iy > 0 && iy < a.ny - 1;
+                const float v = interior ? (2.f * cc[t] - qd) - aa[t] * yy[t] : qd;
+                out[t] = SPONGE ? s * v : v;
+                if (++ix == a.nx) {
+                    ix = 0;
+                    if (++iz == a.nz) { iz = 0; ++iy; }
+                }
+            }
+        }
+        *reinterpret_cast<float4 *>(a.prev + i0) = make_float4(out[0], out[1], out[2], out[3]);
+        *reinterpret_cast<float4 *>(a.y + i0) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (a.nrec > 0) {
+        __shared__ int r_lo, r_hi;
+        __syncthreads();  // this block's new values are visible to the whole block
+        if (threadIdx.x == 0) {
+            const int64_t b0 = (int64_t)blockIdx.x * kUpdateThreads * V;
+            r_lo = lower_bound64(a.rec_node, a.nrec, b0);
+            r_hi = lower_bound64(a.rec_node, a.nrec, b0 + (int64_t)kUpdateThreads * V);
+        }
+        __syncthreads();
+        const int step = a.ctr[1];
+        for (int r = r_lo + threadIdx.x; r < r_hi; r += kUpdateThreads)
+            a.traces[(int64_t)step * a.nrec + a.rec_perm[r]] = a.prev[a.rec_node[r]];
+    }
+}
+
+__global__ void k_connectivity(int32_t *conn, int ex, int ez, int order, int64_t nx, int64_t nz,
+                               int64_t n_elem)
+{
+    const int o1 = order + 1, npe = o1 * o1 * o1;
+    const int64_t total = n_elem * npe;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = q / npe;
+        const int loc = (int)(q - e * npe);
+        const int64_t ix = e % ex, iz = (e / ex) % ez, iy = e / ((int64_t)ex * ez);
+        const int l = loc % o1, n = (loc / o1) % o1, m = loc / (o1 * o1);
+        conn[q] = (int32_t)((ix * order + l) + (iz * order + n) * nx + (iy * order + m) * nx * nz);
+    }
+}
+
+// Elements adjacent to node index i along one axis with ne elements: [lo, hi].
+__device__ __forceinline__ void adj_range(int64_t i, int order, int ne, int64_t &lo, int64_t &hi)
+{
+    const int64_t e = i / order;
+    if (i - e * order == 0) {
+        lo = e > 0 ? e - 1 : 0;
+        hi = e < ne ? e : ne - 1;
+    } else {
+        lo = hi = e;
+    }
+}
+
+__global__ void k_mass(float *a, const float *vel, const float *slow2, int ex, int ey, int ez,
+                       int order, const double *w, double detJ, double dt2)
+{
+    const int64_t nx = (int64_t)ex * order + 1, ny = (int64_t)ey * order + 1,
+                  nz = (int64_t)ez * order + 1, n = nx * ny * nz;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t iy = q / (nx * nz), r = q - iy * nx * nz, iz = r / nx, ix = r - iz * nx;
+        // local weight of the node: w[i mod o] (element-boundary nodes have w_0 = w_o)
+        const double wq = w[ix % order] * w[iz % order] * w[iy % order];
+        int64_t x0, x1, z0, z1, y0, y1;
+        adj_range(ix, order, ex, x0, x1);
+        adj_range(iz, order, ez, z0, z1);
+        adj_range(iy, order, ey, y0, y1);
+        double m;
+        if (slow2) {
+            const double cnt = (double)((x1 - x0 + 1) * (z1 - z0 + 1) * (y1 - y0 + 1));
+            m = (double)slow2[q] * wq * detJ * cnt;
+        } else {
+            double sum = 0.0;
+            for (int64_t ey_ = y0; ey_ <= y1; ey_++)
+                for (int64_t ez_ = z0; ez_ <= z1; ez_++)
+                    for (int64_t ex_ = x0; ex_ <= x1; ex_++) {
+                        const double c = vel[ex_ + ez_ * ex + ey_ * (int64_t)ex * ez];
+                        sum += 1.0 / (c * c);
+                    }
+            m = wq * detJ * sum;
+        }
+        a[q] = (float)(dt2 / m);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_update(const UpdateArgs &a, bool sponge, cudaStream_t s)
+{
+    if (a.n <= 0) return cudaSuccess;
+    const int64_t grid = update_grid(a.n);
+    if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+    if (sponge) k_update<true><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
+    else k_update<false><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_source(const SourceArgs &a, cudaStream_t s)
+{
+    k_source<<<1, 32, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_connectivity(int32_t *conn, int ex, int ey, int ez, int order, cudaStream_t s)
+{
+    const int64_t nx = (int64_t)ex * order + 1, nz = (int64_t)ez * order + 1;
+    const int64_t ne = (int64_t)ex * ey * ez;
+    k_connectivity<<<152 * 16, 256, 0, s>>>(conn, ex, ez, order, nx, nz, ne);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mass(float *a, const float *vel, const float *slow2, int ex, int ey, int ez,
+                        int order, const double *w_dev, double detJ, double dt2, cudaStream_t s)
+{
+    k_mass<<<152 * 16, 256, 0, s>>>(a, vel, slow2, ex, ey, ez, order, w_dev, detJ, dt2);
+    return cudaGetLastError();
+}
+
+}  // namespace semgb

@@ -1,0 +1,315 @@
+"""Python binding of libsemgb (the GB300 SEM acoustic step) over its C ABI (include/semgb.h).
+
+The binding loads ``semgb/_lib/libsemgb.so`` (built by ``proxy-geos-hc_gb300/build.py``) and
+raises if it is missing; there is no other implementation behind it.
+
+Classes mirror the reference's objects: :class:`Mesh` (SEMmesh + the mesh half of
+SEMsolver::computeFEInit) and :class:`Solver` (SEMsolver::computeOneStep in a time loop, with
+source and receiver I/O).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libsemgb.so")
+
+SEM_OK, SEM_ERR_ARG, SEM_ERR_CUDA, SEM_ERR_OOM, SEM_ERR_TIMEOUT, SEM_ERR_UNSTABLE, SEM_ERR_STATE = range(7)
+KERNEL_AUTO, KERNEL_ELEMENT, KERNEL_STENCIL = 0, 1, 2
+LEVEL_CURRENT, LEVEL_PREVIOUS = 0, 1
+
+_I64P = C.POINTER(C.c_int64)
+_I32P = C.POINTER(C.c_int32)
+_F32P = C.POINTER(C.c_float)
+_F64P = C.POINTER(C.c_double)
+_VP = C.c_void_p
+
+
+class SemError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"semgb error {code}: {msg}")
+        self.code = code
+
+
+# name -> argtypes (all functions return int unless listed in _RESTYPE)
+_SIGS = {
+    "sem_last_error_string": [],
+    "sem_version": [],
+    "sem_gll_tables": [C.c_int, _F64P, _F64P, _F64P],
+    "sem_ricker": [C.c_int, C.c_float, C.c_float, C.c_int, _F32P],
+    "sem_box_counts": [C.c_int, C.c_int, C.c_int, C.c_int, _I64P, _I64P, _I64P],
+    "sem_box_connectivity": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64, _I64P],
+    "sem_box_element_from_point": [C.c_int] * 3 + [C.c_float] * 6 + [_I64P],
+    "sem_box_nearest_node": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int] + [C.c_float] * 3 + [_I64P],
+    "sem_box_sponge_profile": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int, C.c_int, C.c_float, _F32P, _F32P, _F32P],
+    "sem_mesh_create_box": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int, C.POINTER(_VP)],
+    "sem_mesh_destroy": [_VP],
+    "sem_mesh_info": [_VP, _I64P, _I64P, C.POINTER(C.c_int), _I64P],
+    "sem_mesh_get_connectivity": [_VP, _I32P],
+    "sem_model_set_element_velocity": [_VP, _F32P],
+    "sem_model_set_node_slowness2": [_VP, _F32P],
+    "sem_solver_create": [_VP, C.c_float, C.POINTER(_VP)],
+    "sem_solver_destroy": [_VP],
+    "sem_solver_set_stream": [_VP, _VP],
+    "sem_solver_set_kernel": [_VP, C.c_int],
+    "sem_solver_set_sponge": [_VP, C.c_int, C.c_float],
+    "sem_solver_set_sponge_profile": [_VP, _F32P, _F32P, _F32P],
+    "sem_solver_set_sources": [_VP, C.c_int, _I64P, _F32P, C.c_int],
+    "sem_solver_set_source_points": [_VP, C.c_int, _F32P, _F32P, C.c_int],
+    "sem_solver_set_receiver_nodes": [_VP, C.c_int, _I64P],
+    "sem_solver_set_receivers": [_VP, C.c_int, _F32P],
+    "sem_solver_step": [_VP, C.c_int],
+    "sem_solver_step_host": [_VP, C.c_int, _F32P, _F32P],
+    "sem_solver_steps_done": [_VP, _I64P],
+    "sem_solver_get_traces": [_VP, _F32P],
+    "sem_solver_get_pressure": [_VP, C.c_int, _F32P],
+    "sem_solver_set_pressure": [_VP, C.c_int, _F32P],
+    "sem_solver_reset": [_VP],
+    "sem_solver_synchronize": [_VP],
+    "sem_solver_time_kernels": [_VP, C.c_int, _F32P],
+}
+_RESTYPE = {"sem_last_error_string": C.c_char_p}
+
+_lib: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    """The loaded libsemgb.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libsemgb.so not built ({LIB_PATH}); run proxy-geos-hc_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        for name, args in _SIGS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = _RESTYPE.get(name, C.c_int)
+        _lib = L
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def _check(rc: int):
+    if rc != SEM_OK:
+        raise SemError(rc, lib().sem_last_error_string().decode())
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def _i64(a):
+    return np.ascontiguousarray(a, np.int64)
+
+
+# ---- host-only utilities ---------------------------------------------------------------------
+
+def gll_tables(order: int):
+    n = order + 1
+    xi, w, d = np.empty(n), np.empty(n), np.empty(n * n)
+    _check(lib().sem_gll_tables(order, _p(xi, _F64P), _p(w, _F64P), _p(d, _F64P)))
+    return xi, w, d.reshape(n, n)
+
+
+def ricker(nsamples: int, dt: float, f0: float, order: int = 1) -> np.ndarray:
+    out = np.empty(nsamples, np.float32)
+    _check(lib().sem_ricker(nsamples, dt, f0, order, _p(out, _F32P)))
+    return out
+
+
+def box_counts(ex, ey, ez, order):
+    a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+    _check(lib().sem_box_counts(ex, ey, ez, order, C.byref(a), C.byref(b), C.byref(c)))
+    return a.value, b.value, c.value
+
+
+def box_connectivity(ex, ey, ez, order, e0=0, count=None):
+    _, ne, _ = box_counts(ex, ey, ez, order)
+    count = ne - e0 if count is None else count
+    out = np.empty((count, (order + 1) ** 3), np.int64)
+    _check(lib().sem_box_connectivity(ex, ey, ez, order, e0, count, _p(out, _I64P)))
+    return out
+
+
+def element_from_point(ex, ey, ez, lx, ly, lz, x, y, z) -> int:
+    e = C.c_int64()
+    _check(lib().sem_box_element_from_point(ex, ey, ez, lx, ly, lz, x, y, z, C.byref(e)))
+    return e.value
+
+
+def nearest_node(ex, ey, ez, lx, ly, lz, order, x, y, z) -> int:
+    n = C.c_int64()
+    _check(lib().sem_box_nearest_node(ex, ey, ez, lx, ly, lz, order, x, y, z, C.byref(n)))
+    return n.value
+
+
+def sponge_profile(ex, ey, ez, lx, ly, lz, order, thickness, sigma):
+    f = [np.empty(n * order + 1, np.float32) for n in (ex, ey, ez)]
+    _check(lib().sem_box_sponge_profile(ex, ey, ez, lx, ly, lz, order, thickness, sigma,
+                                        *[_p(a, _F32P) for a in f]))
+    return tuple(f)
+
+
+# ---- device objects ---------------------------------------------------------------------------
+
+class Mesh:
+    """Structured hex box on the GPU (SEMmesh + the FE set-up of SEMsolver::computeFEInit)."""
+
+    def __init__(self, ex, ey, ez, lx, ly, lz, order):
+        h = _VP()
+        _check(lib().sem_mesh_create_box(ex, ey, ez, lx, ly, lz, order, C.byref(h)))
+        self._h = h
+        self.ex, self.ey, self.ez, self.order = ex, ey, ez, order
+        self.lx, self.ly, self.lz = lx, ly, lz
+        n, e, npe, ni = C.c_int64(), C.c_int64(), C.c_int(), C.c_int64()
+        _check(lib().sem_mesh_info(h, C.byref(n), C.byref(e), C.byref(npe), C.byref(ni)))
+        self.n_nodes, self.n_elem, self.nodes_per_elem, self.n_interior = n.value, e.value, npe.value, ni.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sem_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def connectivity(self) -> np.ndarray:
+        out = np.empty((self.n_elem, self.nodes_per_elem), np.int32)
+        _check(lib().sem_mesh_get_connectivity(self._h, _p(out, _I32P)))
+        return out
+
+    def set_velocity(self, vel):
+        v = _f32(vel)
+        assert v.size == self.n_elem
+        _check(lib().sem_model_set_element_velocity(self._h, _p(v, _F32P)))
+
+    def set_slowness2(self, m):
+        v = _f32(m)
+        assert v.size == self.n_nodes
+        _check(lib().sem_model_set_node_slowness2(self._h, _p(v, _F32P)))
+
+
+class Solver:
+    """Time stepper over a :class:`Mesh` (SEMsolver::computeOneStep + SEMproxy::run's loop)."""
+
+    def __init__(self, mesh: Mesh, dt: float):
+        h = _VP()
+        _check(lib().sem_solver_create(mesh._h, dt, C.byref(h)))
+        self._h = h
+        self.mesh = mesh
+        self.dt = dt
+        self.nrec = 0
+        self.nsrc = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sem_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        _check(lib().sem_solver_set_stream(self._h, stream_handle))
+
+    def set_kernel(self, kernel: int):
+        _check(lib().sem_solver_set_kernel(self._h, kernel))
+
+    def set_sponge(self, thickness: int, sigma: float):
+        _check(lib().sem_solver_set_sponge(self._h, thickness, sigma))
+
+    def set_sponge_profile(self, sx, sy, sz):
+        a, b, c = _f32(sx), _f32(sy), _f32(sz)
+        _check(lib().sem_solver_set_sponge_profile(self._h, _p(a, _F32P), _p(b, _F32P), _p(c, _F32P)))
+
+    def set_sources(self, elements, wavelet):
+        e = _i64(elements)
+        w = _f32(wavelet).reshape(len(e), -1) if len(e) else np.zeros((0, 0), np.float32)
+        _check(lib().sem_solver_set_sources(self._h, len(e), _p(e, _I64P), _p(w, _F32P), w.shape[1]))
+        self.nsrc = len(e)
+
+    def set_source_points(self, xyz, wavelet):
+        x = _f32(xyz).reshape(-1, 3)
+        w = _f32(wavelet).reshape(len(x), -1)
+        _check(lib().sem_solver_set_source_points(self._h, len(x), _p(x, _F32P), _p(w, _F32P), w.shape[1]))
+        self.nsrc = len(x)
+
+    def set_receiver_nodes(self, nodes):
+        n = _i64(nodes)
+        _check(lib().sem_solver_set_receiver_nodes(self._h, len(n), _p(n, _I64P)))
+        self.nrec = len(n)
+
+    def set_receivers(self, xyz):
+        x = _f32(xyz).reshape(-1, 3)
+        _check(lib().sem_solver_set_receivers(self._h, len(x), _p(x, _F32P)))
+        self.nrec = len(x)
+
+    def step(self, n: int = 1):
+        _check(lib().sem_solver_step(self._h, n))
+
+    def step_host(self, n: int, wavelet_samples=None, traces_out=None):
+        w = _f32(wavelet_samples) if wavelet_samples is not None else None
+        _check(lib().sem_solver_step_host(self._h, n, _p(w, _F32P) if w is not None else None,
+                                          _p(traces_out, _F32P) if traces_out is not None else None))
+
+    @property
+    def steps_done(self) -> int:
+        n = C.c_int64()
+        _check(lib().sem_solver_steps_done(self._h, C.byref(n)))
+        return n.value
+
+    def traces(self) -> np.ndarray:
+        out = np.zeros((self.steps_done, self.nrec), np.float32)
+        _check(lib().sem_solver_get_traces(self._h, _p(out, _F32P)))
+        return out
+
+    def pressure(self, level: int = LEVEL_CURRENT) -> np.ndarray:
+        out = np.empty(self.mesh.n_nodes, np.float32)
+        _check(lib().sem_solver_get_pressure(self._h, level, _p(out, _F32P)))
+        return out
+
+    def set_pressure(self, level: int, values):
+        v = _f32(values)
+        _check(lib().sem_solver_set_pressure(self._h, level, _p(v, _F32P)))
+
+    def reset(self):
+        _check(lib().sem_solver_reset(self._h))
+
+    def synchronize(self):
+        _check(lib().sem_solver_synchronize(self._h))
+
+    def time_kernels(self, n: int) -> np.ndarray:
+        ms = np.zeros(3, np.float32)
+        _check(lib().sem_solver_time_kernels(self._h, n, _p(ms, _F32P)))
+        return ms
+
+
+def solver_from_workload(wl, kernel: int = KERNEL_AUTO):
+    """Build (mesh, solver) for a :class:`semgb.workloads.Workload`, resolving positions with
+    the library's own host logic."""
+    mesh = Mesh(wl.ex, wl.ey, wl.ez, wl.lx, wl.ly, wl.lz, wl.order)
+    mesh.set_velocity(wl.vel)
+    s = Solver(mesh, wl.dt)
+    s.set_kernel(kernel)
+    if wl.sponge_thickness > 0:
+        s.set_sponge(wl.sponge_thickness, wl.sponge_sigma)
+    wav = np.stack([ricker(wl.nsteps, wl.dt, float(f), wl.ricker_order) for f in wl.f0])
+    s.set_source_points(wl.src_xyz, wav)
+    s.set_receivers(wl.rec_xyz)
+    return mesh, s
