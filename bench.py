@@ -114,10 +114,10 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def make_workload(name: str):
+def make_workload(name: str, elems: int = 200):
     from semgb import workloads as W
     if name == "c2":
-        return W.c2_plain_scale(200, steps=1000)
+        return W.c2_plain_scale(elems, steps=1000)
     if name == "c1":
         return W.c1_plain_small(1500)
     raise SystemExit(f"unknown workload {name}")
@@ -158,7 +158,7 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    wl = make_workload(args.workload)
+    wl = make_workload(args.workload, args.elems)
     n = args.ref_elems
     sw = cpu_sample(wl, n)
     from oracle import oracle as O
@@ -213,7 +213,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     if ws > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    wl = make_workload(args.workload)
+    wl = make_workload(args.workload, args.elems)
     kernel = {"auto": semgb.KERNEL_AUTO, "element": semgb.KERNEL_ELEMENT,
               "stencil": semgb.KERNEL_STENCIL}[args.kernel]
     mesh, s = semgb.solver_from_workload(wl, kernel)
@@ -247,7 +247,7 @@ def run_ours(args):
     value = N * args.steps * ws / (t_max / 1e3) / 1e9
 
     # per-kernel device time (CUDA events on the solver's stream, un-captured launches)
-    kms = s.time_kernels(max(5, min(20, args.steps)))
+    kms = [float(x) for x in s.time_kernels(max(5, min(20, args.steps)))]
     resolved = "stencil" if kernel in (semgb.KERNEL_AUTO, semgb.KERNEL_STENCIL) else "element"
     peak, peak_kind = hbm_peak()
     if resolved == "stencil":
@@ -340,6 +340,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["c2", "c1"], default="c2")
     ap.add_argument("--kernel", choices=["auto", "element", "stencil"], default="auto")
+    ap.add_argument("--elems", type=int, default=200, help="elements per axis of the c2 recipe")
     ap.add_argument("--cpu-elems", type=int, default=40, help="cpu_baseline sub-box (elements per axis)")
     ap.add_argument("--cpu-steps", type=int, default=16, help="cpu_baseline steps")
     ap.add_argument("--ref-elems", type=int, default=32, help="--impl reference sub-box (elements per axis)")

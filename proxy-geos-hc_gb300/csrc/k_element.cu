@@ -10,9 +10,10 @@
 // contraction is written in difference form so that a constant field gives exactly zero (the
 // float-rounded derivative table does not sum exactly to zero per row).
 //
-// CTA shape: kElemTile (32) elements x (o+1)^2 warps.  Lane = element of the tile; warp = pencil.
-// All lanes of a warp work on the same local pencil of different elements, so every coefficient
-// index is warp-uniform and shared-memory accesses are unit-stride in the lane.  Phases:
+// CTA shape: TE elements x (o+1)^2 pencils, thread = (pencil, element); TE = 32 (one element per
+// lane, one pencil per warp) for orders 1-4 and 16 for order 5 (36 pencils would exceed 1024
+// threads).  All lanes of a warp work on the same local pencil of different elements, so
+// coefficient indices are warp-uniform and shared-memory accesses are unit-stride.  Phases:
 //   A  the CTA's 32 connectivity rows (contiguous in HBM) -> shared, coalesced
 //   B  gather p through the rows: each thread loads its x-pencil (registers + shared copy)
 //   C  x-direction contraction in registers
@@ -32,10 +33,11 @@ namespace {
 template <int O>
 struct ElemCfg {
     static constexpr int O1 = O + 1, NP = O1 * O1, NPE = O1 * O1 * O1;
+    static constexpr int TE = O <= 4 ? 32 : 16;  // elements per CTA
     static constexpr int CS = NPE | 1;  // odd row stride: lanes hit distinct banks
-    static constexpr int THREADS = 32 * NP;
-    static constexpr int MINB = O == 1 ? 8 : O == 2 ? 5 : O == 3 ? 3 : O == 4 ? 2 : 1;
-    static constexpr size_t SMEM = sizeof(int) * kElemTile * CS + sizeof(float) * NPE * kElemTile * 2 +
+    static constexpr int THREADS = TE * NP;
+    static constexpr int MINB = O == 1 ? 8 : O == 2 ? 5 : O == 3 ? 3 : O == 4 ? 2 : 2;
+    static constexpr size_t SMEM = sizeof(int) * TE * CS + sizeof(float) * NPE * TE * 2 +
                                    sizeof(float) * 3 * NP;
 };
 
@@ -68,14 +70,15 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     k_element(const ElementArgs a)
 {
     using C = ElemCfg<O>;
-    constexpr int O1 = C::O1, NP = C::NP, NPE = C::NPE, CS = C::CS, TE = kElemTile;
+    constexpr int O1 = C::O1, NP = C::NP, NPE = C::NPE, CS = C::CS, TE = C::TE;
     extern __shared__ __align__(16) unsigned char smem[];
     int *s_conn = reinterpret_cast<int *>(smem);
     float *s_p = reinterpret_cast<float *>(s_conn + TE * CS);
     float *s_y = s_p + NPE * TE;
     float *s_tab = s_y + NPE * TE;
 
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // "lane" = element of the tile, "warp" = pencil (a hardware warp when TE == 32)
+    const int tid = threadIdx.x, lane = tid % TE, warp = tid / TE;
     const int64_t e0 = (int64_t)blockIdx.x * TE;
     const int ne = (int)min((int64_t)TE, a.n_elem - e0);
 
@@ -151,7 +154,7 @@ cudaError_t launch_element_t(const ElementArgs &a, cudaStream_t s)
 {
     using C = ElemCfg<O>;
     if (a.n_elem <= 0) return cudaSuccess;
-    const int64_t grid = (a.n_elem + kElemTile - 1) / kElemTile;
+    const int64_t grid = (a.n_elem + C::TE - 1) / C::TE;
     if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
     k_element<O><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(a);
     return cudaGetLastError();

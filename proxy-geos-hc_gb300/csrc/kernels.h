@@ -14,8 +14,6 @@
 
 namespace semgb {
 
-constexpr int kElemTile = 32;  // elements per CTA in the element kernel (one per lane)
-
 // Uniform-box geometry: J = diag(hx/2, hz/2, hy/2) for the reference directions
 // (xi1 -> x, xi2 -> z, xi3 -> y).  g[d] = |detJ| / J_dd^2 (the diagonal of B, SEMQkGLIntegrals
 // .hpp:344-349); off-diagonal terms are exactly zero on this mesh.
