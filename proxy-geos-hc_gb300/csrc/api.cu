@@ -59,8 +59,6 @@ static void dfree(T *&p)
     p = nullptr;
 }
 
-static int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
-
 // ----------------------------------------------------------------------------------------------
 // handles
 // ----------------------------------------------------------------------------------------------
@@ -82,7 +80,7 @@ struct sem_solver {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int kernel = SEM_KERNEL_AUTO;
-    int64_t n4 = 0;
+    int64_t n_int = 0;               // nodes of the device layout
     float *d_p[2] = {nullptr, nullptr};
     int cur = 0;                 // index of the current level
     float *d_y = nullptr;        // element path accumulator
@@ -105,10 +103,15 @@ struct sem_solver {
     int nrec = 0;
     int64_t *d_rec_node = nullptr;  // sorted by node
     int *d_rec_perm = nullptr;      // sorted position -> caller's receiver index
+    std::vector<int64_t> rec_sorted;
+    uint64_t rec_version = 1;
     float *d_traces = nullptr;      // [trace_cap][nrec]
     int64_t trace_cap = 0;
     int64_t traces_checked = 0;
     int *d_ctr = nullptr;           // [0] next step, [1] step in flight
+    int *d_status = nullptr;        // non-zero after a bounded device wait gave up
+    int *d_upd_rec_off = nullptr;   // receivers grouped by update-kernel block
+    uint64_t upd_rec_version = 0;
     int64_t steps_done = 0;
     // graphs: [parity] two steps starting at level `parity`
     cudaGraphExec_t graph2[2] = {nullptr, nullptr};
@@ -277,10 +280,10 @@ int sem_mesh_info(const sem_mesh *m, int64_t *n_nodes, int64_t *n_elem, int *npe
 static int ensure_conn(sem_mesh *m, cudaStream_t s)
 {
     if (m->d_conn) return SEM_OK;
-    if (m->box.n_nodes > 0x7fffffffLL)
+    if (m->box.n_int > 0x7fffffffLL)
         return fail(SEM_ERR_ARG, "element kernel needs fewer than 2^31 nodes (int32 connectivity)");
     CUDA_TRY(dalloc(&m->d_conn, (size_t)m->box.n_elem * m->box.npe));
-    CUDA_TRY(launch_connectivity(m->d_conn, m->box.ex, m->box.ey, m->box.ez, m->box.order, s));
+    CUDA_TRY(launch_connectivity(m->d_conn, m->box.ex, m->box.ey, m->box.ez, m->box.order, m->box.nxp, s));
     return SEM_OK;
 }
 
@@ -290,8 +293,9 @@ int sem_mesh_get_connectivity(sem_mesh *m, int32_t *conn)
     if (!m || !conn) return fail(SEM_ERR_ARG, "NULL argument");
     int rc = ensure_conn(m, 0);
     if (rc) return rc;
-    CUDA_TRY(cudaMemcpy(conn, m->d_conn, (size_t)m->box.n_elem * m->box.npe * sizeof(int32_t),
-                        cudaMemcpyDeviceToHost));
+    const size_t n = (size_t)m->box.n_elem * m->box.npe;
+    CUDA_TRY(cudaMemcpy(conn, m->d_conn, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) conn[i] = (int32_t)to_reference(m->box, conn[i]);  // device -> reference numbering
     return SEM_OK;
     GUARD_END
 }
@@ -318,8 +322,12 @@ int sem_model_set_node_slowness2(sem_mesh *m, const float *s2)
     for (int64_t i = 0; i < m->box.n_nodes; i++)
         if (!(s2[i] > 0) || !std::isfinite(s2[i]))
             return fail(SEM_ERR_ARG, "squared slowness must be positive and finite");
-    if (!m->d_slow2) CUDA_TRY(dalloc(&m->d_slow2, m->box.n_nodes));
-    CUDA_TRY(cudaMemcpy(m->d_slow2, s2, m->box.n_nodes * sizeof(float), cudaMemcpyHostToDevice));
+    if (!m->d_slow2) {
+        CUDA_TRY(dalloc(&m->d_slow2, m->box.n_int));
+        CUDA_TRY(cudaMemset(m->d_slow2, 0, m->box.n_int * 4));
+    }
+    CUDA_TRY(cudaMemcpy2D(m->d_slow2, m->box.nxp * 4, s2, m->box.nx * 4, m->box.nx * 4,
+                          m->box.nz * m->box.ny, cudaMemcpyHostToDevice));
     m->model_version++;
     return SEM_OK;
     GUARD_END
@@ -350,6 +358,8 @@ int sem_solver_destroy(sem_solver *s)
     dfree(s->d_rec_perm);
     dfree(s->d_traces);
     dfree(s->d_ctr);
+    dfree(s->d_status);
+    dfree(s->d_upd_rec_off);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return SEM_OK;
@@ -364,7 +374,7 @@ int sem_solver_create(sem_mesh *m, float dt, sem_solver **out)
     sem_solver *s = new sem_solver();
     s->mesh = m;
     s->dt = dt;
-    s->n4 = pad4(m->box.n_nodes);
+    s->n_int = m->box.n_int;
     auto cleanup = [&](int code, const std::string &msg) {
         sem_solver_destroy(s);
         return fail(code, msg);
@@ -373,11 +383,13 @@ int sem_solver_create(sem_mesh *m, float dt, sem_solver **out)
     if (e != cudaSuccess) return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     s->own_stream = true;
     for (auto &p : s->d_p)
-        if ((e = dalloc(&p, s->n4)) != cudaSuccess || (e = cudaMemset(p, 0, s->n4 * 4)) != cudaSuccess)
+        if ((e = dalloc(&p, s->n_int)) != cudaSuccess || (e = cudaMemset(p, 0, s->n_int * 4)) != cudaSuccess)
             return cleanup(SEM_ERR_OOM, std::string("pressure levels: ") + cudaGetErrorString(e));
-    if ((e = dalloc(&s->d_a, s->n4)) != cudaSuccess || (e = cudaMemset(s->d_a, 0, s->n4 * 4)) != cudaSuccess)
+    if ((e = dalloc(&s->d_a, s->n_int)) != cudaSuccess || (e = cudaMemset(s->d_a, 0, s->n_int * 4)) != cudaSuccess)
         return cleanup(SEM_ERR_OOM, std::string("mass coefficient: ") + cudaGetErrorString(e));
     if ((e = dalloc(&s->d_ctr, 2)) != cudaSuccess || (e = cudaMemset(s->d_ctr, 0, 8)) != cudaSuccess)
+        return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
+    if ((e = dalloc(&s->d_status, 1)) != cudaSuccess || (e = cudaMemset(s->d_status, 0, 4)) != cudaSuccess)
         return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     if ((e = dalloc(&s->d_w, m->box.order + 1)) != cudaSuccess ||
         (e = cudaMemcpy(s->d_w, m->gll.w, (m->box.order + 1) * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -486,7 +498,7 @@ int sem_solver_set_sources(sem_solver *s, int n_src, const int64_t *elements, co
     for (int k = 0; k < n_src; k++) {
         if (elements[k] < 0 || elements[k] >= b.n_elem)
             return fail(SEM_ERR_ARG, "source element out of range");
-        node[k] = box_node(b, elements[k], 0);  // local node 0 (SEMsolver.cpp:40)
+        node[k] = to_internal(b, box_node(b, elements[k], 0));  // local node 0 (SEMsolver.cpp:40)
         const float c = vel[elements[k]];
         coef[k] = dt * dt * c * c;              // rounded as SEMsolver.cpp:41-42
     }
@@ -537,8 +549,8 @@ int sem_solver_set_receiver_nodes(sem_solver *s, int n_rec, const int64_t *nodes
     std::vector<int> perm(n_rec);
     std::iota(perm.begin(), perm.end(), 0);
     std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return nodes[a] < nodes[b]; });
-    std::vector<int64_t> sorted(n_rec);
-    for (int r = 0; r < n_rec; r++) sorted[r] = nodes[perm[r]];
+    std::vector<int64_t> sorted(n_rec);  // device-layout indices (same order as reference indices)
+    for (int r = 0; r < n_rec; r++) sorted[r] = to_internal(s->mesh->box, nodes[perm[r]]);
     cudaStreamSynchronize(s->stream);
     invalidate_graphs(s);
     dfree(s->d_rec_node);
@@ -547,6 +559,8 @@ int sem_solver_set_receiver_nodes(sem_solver *s, int n_rec, const int64_t *nodes
     s->trace_cap = 0;
     s->traces_checked = 0;
     s->nrec = n_rec;
+    s->rec_sorted = sorted;
+    s->rec_version++;
     if (n_rec > 0) {
         CUDA_TRY(dalloc(&s->d_rec_node, n_rec));
         CUDA_TRY(dalloc(&s->d_rec_perm, n_rec));
@@ -576,19 +590,41 @@ static int prepare(sem_solver *s, int64_t n_new)
     const int kern = resolved_kernel(s);
     if (s->a_version != m->model_version) {
         CUDA_TRY(launch_mass(s->d_a, m->d_slow2 ? nullptr : m->d_vel, m->d_slow2, m->box.ex, m->box.ey,
-                             m->box.ez, m->box.order, s->d_w, m->geo.detJ, (double)s->dt * s->dt, s->stream));
+                             m->box.ez, m->box.order, m->box.nxp, s->d_w, m->geo.detJ,
+                             (double)s->dt * s->dt, s->stream));
         s->a_version = m->model_version;
     }
     if (kern == SEM_KERNEL_ELEMENT) {
         int rc = ensure_conn(m, s->stream);
         if (rc) return rc;
         if (!s->d_y) {
-            CUDA_TRY(dalloc(&s->d_y, s->n4));
-            CUDA_TRY(cudaMemsetAsync(s->d_y, 0, s->n4 * 4, s->stream));
+            CUDA_TRY(dalloc(&s->d_y, s->n_int));
+            CUDA_TRY(cudaMemsetAsync(s->d_y, 0, s->n_int * 4, s->stream));
         }
-    } else if (!s->stencil) {
-        int rc = stencil_tables_create(m->box, m->gll, m->geo, &s->stencil);
-        if (rc) return fail(SEM_ERR_CUDA, "stencil tables: " + std::string(cudaGetErrorString((cudaError_t)rc)));
+        if (s->upd_rec_version != s->rec_version) {
+            dfree(s->d_upd_rec_off);
+            if (s->nrec > 0) {
+                const int64_t nb = update_grid(s->n_int);
+                std::vector<int> off(nb + 1, 0);
+                for (int64_t q : s->rec_sorted) off[q / kUpdateNodesPerBlock + 1]++;
+                for (int64_t b = 0; b < nb; b++) off[b + 1] += off[b];
+                CUDA_TRY(dalloc(&s->d_upd_rec_off, nb + 1));
+                CUDA_TRY(cudaMemcpy(s->d_upd_rec_off, off.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
+            }
+            s->upd_rec_version = s->rec_version;
+            invalidate_graphs(s);
+        }
+    } else {
+        if (!s->stencil) {
+            int rc = stencil_tables_create(m->box, m->gll, m->geo, &s->stencil);
+            if (rc) return fail(SEM_ERR_CUDA, "stencil tables");
+        }
+        if (stencil_bind(*s->stencil, s->d_p[0], s->d_p[1], s->d_a) != 0)
+            return fail(SEM_ERR_CUDA, "tensor-map encoding failed (driver entry point cuTensorMapEncodeTiled)");
+        if (s->stencil->rec_version != s->rec_version) {
+            CUDA_TRY(stencil_set_receivers(*s->stencil, s->rec_sorted.data(), s->nrec, s->rec_version));
+            invalidate_graphs(s);
+        }
     }
     if (s->nrec > 0 && s->steps_done + n_new > s->trace_cap) {
         int64_t cap = std::max<int64_t>(s->steps_done + n_new, std::max<int64_t>(64, 2 * s->trace_cap));
@@ -639,9 +675,10 @@ static cudaError_t enqueue_step(sem_solver *s, int c, cudaEvent_t *ev = nullptr)
         ua.y = s->d_y;
         ua.a = s->d_a;
         ua.sx = s->d_sx; ua.sy = s->d_sy; ua.sz = s->d_sz;
-        ua.nx = b.nx; ua.ny = b.ny; ua.nz = b.nz; ua.n = b.n_nodes;
+        ua.nx = b.nx; ua.nxp = b.nxp; ua.ny = b.ny; ua.nz = b.nz; ua.n_int = b.n_int;
         ua.rec_node = s->d_rec_node;
         ua.rec_perm = s->d_rec_perm;
+        ua.rec_off = s->d_upd_rec_off;
         ua.nrec = s->nrec;
         ua.traces = s->d_traces;
         ua.ctr = s->d_ctr;
@@ -650,14 +687,16 @@ static cudaError_t enqueue_step(sem_solver *s, int c, cudaEvent_t *ev = nullptr)
         StencilArgs ta{};
         ta.cur = s->d_p[c];
         ta.prev = s->d_p[1 - c];
-        ta.a = s->d_a;
         ta.sx = s->d_sx; ta.sy = s->d_sy; ta.sz = s->d_sz;
+        ta.status = s->d_status;
         ta.rec_node = s->d_rec_node;
         ta.rec_perm = s->d_rec_perm;
+        ta.rec_off = s->stencil->d_rec_off;
+        ta.rec_idx = s->stencil->d_rec_idx;
         ta.nrec = s->nrec;
         ta.traces = s->d_traces;
         ta.ctr = s->d_ctr;
-        if ((e = launch_stencil(*s->stencil, ta, s->sponge, s->stream)) != cudaSuccess) return e;
+        if ((e = launch_stencil(*s->stencil, ta, c, s->sponge, s->stream)) != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[2], s->stream);
     }
     if (ev) cudaEventRecord(ev[3], s->stream);
@@ -748,6 +787,10 @@ int sem_solver_synchronize(sem_solver *s)
     GUARD_BEGIN
     if (!s) return fail(SEM_ERR_ARG, "NULL solver");
     CUDA_TRY(cudaStreamSynchronize(s->stream));
+    int status = 0;
+    CUDA_TRY(cudaMemcpy(&status, s->d_status, 4, cudaMemcpyDeviceToHost));
+    if (status != 0)
+        return fail(SEM_ERR_TIMEOUT, "a bounded wait for a TMA tile gave up; results of this run are invalid");
     if (s->nrec > 0 && s->steps_done > s->traces_checked) {
         const int64_t n = (s->steps_done - s->traces_checked) * s->nrec;
         std::vector<float> t(n);
@@ -776,6 +819,17 @@ int sem_solver_get_traces(sem_solver *s, float *out)
     GUARD_END
 }
 
+// Per-node sponge factors of the reference layout, as the kernels form them: (sx*sy)*sz.
+static int host_sponge(sem_solver *s, std::vector<float> &sx, std::vector<float> &sy, std::vector<float> &sz)
+{
+    const Box &b = s->mesh->box;
+    sx.resize(b.nx); sy.resize(b.ny); sz.resize(b.nz);
+    CUDA_TRY(cudaMemcpy(sx.data(), s->d_sx, b.nx * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(sy.data(), s->d_sy, b.ny * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(sz.data(), s->d_sz, b.nz * 4, cudaMemcpyDeviceToHost));
+    return SEM_OK;
+}
+
 int sem_solver_get_pressure(sem_solver *s, int level, float *out)
 {
     GUARD_BEGIN
@@ -784,13 +838,13 @@ int sem_solver_get_pressure(sem_solver *s, int level, float *out)
     const Box &b = s->mesh->box;
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     const int idx = level == SEM_LEVEL_CURRENT ? s->cur : 1 - s->cur;
-    CUDA_TRY(cudaMemcpy(out, s->d_p[idx], b.n_nodes * 4, cudaMemcpyDeviceToHost));
+    // device layout (rows of nxp) -> reference layout (rows of nx)
+    CUDA_TRY(cudaMemcpy2D(out, b.nx * 4, s->d_p[idx], b.nxp * 4, b.nx * 4, b.nz * b.ny, cudaMemcpyDeviceToHost));
     if (level == SEM_LEVEL_PREVIOUS && s->sponge) {
         // the stored previous level still lacks its last sponge factor
-        std::vector<float> sx(b.nx), sy(b.ny), sz(b.nz);
-        CUDA_TRY(cudaMemcpy(sx.data(), s->d_sx, b.nx * 4, cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(sy.data(), s->d_sy, b.ny * 4, cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(sz.data(), s->d_sz, b.nz * 4, cudaMemcpyDeviceToHost));
+        std::vector<float> sx, sy, sz;
+        int rc = host_sponge(s, sx, sy, sz);
+        if (rc) return rc;
         int64_t i = 0;
         for (int64_t iy = 0; iy < b.ny; iy++)
             for (int64_t iz = 0; iz < b.nz; iz++)
@@ -815,10 +869,9 @@ int sem_solver_set_pressure(sem_solver *s, int level, const float *in)
     if (level == SEM_LEVEL_PREVIOUS && s->sponge) {
         // stored without its last sponge factor: divide it out where it is non-zero, so that the
         // next step sees (to within one rounding) the damped level the caller passed
-        std::vector<float> sx(b.nx), sy(b.ny), sz(b.nz);
-        CUDA_TRY(cudaMemcpy(sx.data(), s->d_sx, b.nx * 4, cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(sy.data(), s->d_sy, b.ny * 4, cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(sz.data(), s->d_sz, b.nz * 4, cudaMemcpyDeviceToHost));
+        std::vector<float> sx, sy, sz;
+        int rc = host_sponge(s, sx, sy, sz);
+        if (rc) return rc;
         int64_t i = 0;
         for (int64_t iy = 0; iy < b.ny; iy++)
             for (int64_t iz = 0; iz < b.nz; iz++)
@@ -827,7 +880,7 @@ int sem_solver_set_pressure(sem_solver *s, int level, const float *in)
                     if (f > 0) v[i] = v[i] / f;
                 }
     }
-    CUDA_TRY(cudaMemcpy(s->d_p[idx], v.data(), b.n_nodes * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy2D(s->d_p[idx], b.nxp * 4, v.data(), b.nx * 4, b.nx * 4, b.nz * b.ny, cudaMemcpyHostToDevice));
     return SEM_OK;
     GUARD_END
 }
@@ -837,9 +890,10 @@ int sem_solver_reset(sem_solver *s)
     GUARD_BEGIN
     if (!s) return fail(SEM_ERR_ARG, "NULL solver");
     CUDA_TRY(cudaStreamSynchronize(s->stream));
-    for (auto p : s->d_p) CUDA_TRY(cudaMemset(p, 0, s->n4 * 4));
-    if (s->d_y) CUDA_TRY(cudaMemset(s->d_y, 0, s->n4 * 4));
+    for (auto p : s->d_p) CUDA_TRY(cudaMemset(p, 0, s->n_int * 4));
+    if (s->d_y) CUDA_TRY(cudaMemset(s->d_y, 0, s->n_int * 4));
     CUDA_TRY(cudaMemset(s->d_ctr, 0, 8));
+    CUDA_TRY(cudaMemset(s->d_status, 0, 4));
     if (s->d_traces) CUDA_TRY(cudaMemset(s->d_traces, 0, (size_t)s->trace_cap * s->nrec * 4));
     s->steps_done = 0;
     s->traces_checked = 0;

@@ -99,6 +99,8 @@ bool make_box(int ex, int ey, int ez, float lx, float ly, float lz, int order, B
     b.n_elem = (int64_t)ex * ey * ez;
     b.n_interior = (b.nx - 2) * (b.ny - 2) * (b.nz - 2);
     b.npe = (order + 1) * (order + 1) * (order + 1);
+    b.nxp = (b.nx + kRowAlign - 1) / kRowAlign * kRowAlign;
+    b.n_int = b.nxp * b.nz * b.ny;
     return true;
 }
 

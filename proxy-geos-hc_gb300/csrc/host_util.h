@@ -23,13 +23,34 @@ bool gll_tables(int order, Gll &g);
 // Ricker wavelet in the reference's float arithmetic (utils.hpp:11-46).
 float ricker(float t, float f0, int order);
 
+// Device layout: rows along x are padded to nxp = nx rounded up to 32 floats (128 bytes), so
+// every row starts on a 128-byte boundary (vector accesses and TMA tiles); internal node index
+// = ix + iz*nxp + iy*nxp*nz.  Padding nodes hold zero.  The ABI speaks the reference numbering.
+constexpr int kRowAlign = 32;
+
 struct Box {
     int ex = 0, ey = 0, ez = 0, order = 0;
     float lx = 0, ly = 0, lz = 0;
     int64_t nx = 0, ny = 0, nz = 0;  // nodes per axis
     int64_t n_nodes = 0, n_elem = 0, n_interior = 0;
     int npe = 0;                    // nodes per element
+    int64_t nxp = 0;                // padded row length of the device layout
+    int64_t n_int = 0;              // nodes in the device layout, nxp*nz*ny
 };
+
+// Reference node index -> device-layout index.
+inline int64_t to_internal(const Box &b, int64_t node)
+{
+    const int64_t iy = node / (b.nx * b.nz), r = node - iy * b.nx * b.nz, iz = r / b.nx, ix = r - iz * b.nx;
+    return ix + iz * b.nxp + iy * b.nxp * b.nz;
+}
+
+// Device-layout index -> reference node index (the index must not be a padding node).
+inline int64_t to_reference(const Box &b, int64_t q)
+{
+    const int64_t iy = q / (b.nxp * b.nz), r = q - iy * b.nxp * b.nz, iz = r / b.nxp, ix = r - iz * b.nxp;
+    return ix + iz * b.nx + iy * b.nx * b.nz;
+}
 
 bool make_box(int ex, int ey, int ez, float lx, float ly, float lz, int order, Box &b);
 

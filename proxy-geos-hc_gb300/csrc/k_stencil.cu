@@ -1,24 +1,63 @@
-// k_stencil.cu -- fused SEM step on a uniform box (see stencil.h for the operator).
+// k_stencil.cu -- fused SEM step on a uniform box (operator in stencil.h), TMA-pipelined.
 //
-// One thread per node.  For each axis the assembled 1-D stiffness row of a node depends only on
-// its local index l = i mod o inside the element, so the three axis terms use one table
+// Coefficients: for each axis the assembled 1-D stiffness row of a node depends only on its local
+// index l = i mod o, so the three axis terms use one table
 //     T[l][d + o] = coupling between a node with local index l and the node d places further
-// along the same axis (d in [-o, o]; zero outside the node's element or element pair), applied
-// in difference form sum_d T[l][d] (p_{i+d} - p_i), which is exactly zero for a constant field.
+// along the same axis (zero outside the node's element or element pair), applied in difference
+// form sum_d T[l][d] (p_{i+d} - p_i), exactly zero for a constant field.
+//
+// Work decomposition (HBM-bound pass: read p^n, p^{n-1}, dt^2/M, write p^{n+1}; 16 B/node):
+//  - a CTA owns a tile of TX = 32*o nodes along x by TZ rows along z and marches along y over a
+//    chunk of planes; warp = row, lane = one element's o consecutive x-nodes, so a node's local x
+//    index is a compile-time constant (x-coefficients are immediates, zero terms are skipped);
+//    the z- and y-local indices are warp-uniform and select specialised code;
+//  - one elected thread streams y-planes into shared memory with 3-D TMA tile loads completed on
+//    mbarriers: a ring of 2o+1+L planes of p^n (tile rows with an x halo) serves the x- and
+//    y-neighbours, and per-plane "aux" slots hold the z-halo rows of p^n plus the p^{n-1} and
+//    dt^2/M tiles; loads run L planes ahead of the compute;
+//  - one barrier per plane; every mbarrier wait is bounded (tma.cuh) and a timeout is reported
+//    through a status word instead of hanging.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
 #include "stencil.h"
+#include "tma.cuh"
 
 namespace semgb {
 
 namespace {
 
-constexpr int kStencilThreads = 256;
-constexpr int kTMax = 5 * 5 * 11;
+constexpr int kLook = 2;                   // planes of lookahead
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+constexpr int kTMax = kMaxOrder * (2 * kMaxOrder + 1);
 __constant__ float c_T[kMaxOrder][kTMax];  // [order-1][l * (2o+1) + d + o]
+__constant__ float c_wa[kMaxOrder][kMaxOrder];  // assembled weights by local index
+
+template <int O>
+struct Cfg {
+    static constexpr int TZ = O == 5 ? 8 : 16;          // rows (warps) per CTA
+    static constexpr int THREADS = 32 * TZ;
+    static constexpr int TX = 32 * O;                   // nodes along x per CTA
+    static constexpr int HX = O <= 4 ? 4 : 8;           // x halo, a multiple of 4 floats
+    static constexpr int TXP = TX + 2 * HX;             // ring row length
+    static constexpr int TZP = TZ + 2 * O;              // ring rows: tile plus z halo
+    static constexpr int W = 2 * O + 1;
+    static constexpr int R = W + kLook;                 // ring slots
+    static constexpr int AUX = kLook + 1;               // aux slots
+    static constexpr size_t al(size_t b) { return (b + 127) / 128 * 128; }
+    static constexpr int RING_FLOATS = (int)(al(sizeof(float) * TZP * TXP) / 4);
+    static constexpr int TILE_FLOATS = (int)(al(sizeof(float) * TZ * TX) / 4);
+    static constexpr int AUX_FLOATS = 2 * TILE_FLOATS;  // p^{n-1} tile, dt^2/M tile
+    static constexpr size_t OFF_AUX = (size_t)R * RING_FLOATS * 4;
+    static constexpr size_t OFF_BAR = OFF_AUX + (size_t)AUX * AUX_FLOATS * 4;
+    static constexpr size_t SMEM = OFF_BAR + 8 * (R + AUX);
+    static constexpr uint32_t RING_TX = sizeof(float) * TZP * TXP;
+    static constexpr uint32_t AUX_TX = sizeof(float) * 2 * TZ * TX;
+};
 
 // Host: T for one order from the GLL tables (double, rounded once).
 void build_T(const Gll &g, float *T)
@@ -45,76 +84,329 @@ void build_T(const Gll &g, float *T)
         }
 }
 
-template <int O, bool SPONGE>
-__global__ void __launch_bounds__(kStencilThreads) k_stencil_simple(const StencilTables t, const StencilArgs a)
-{
-    constexpr int W = 2 * O + 1;
-    __shared__ float sT[O * W];
-    __shared__ float sW[O];
-    for (int q = threadIdx.x; q < O * W; q += kStencilThreads) sT[q] = c_T[O - 1][q];
-#pragma unroll
-    for (int l = 0; l < O; l++)  // static indices keep the parameter struct out of local memory
-        if (threadIdx.x == l) sW[l] = t.wa[l];
-    __syncthreads();
+// Offsets d with a non-zero coefficient for local index l: [-o, o] for l == 0 (element face),
+// [-l, o-l] otherwise.
+__host__ __device__ constexpr int dlo(int O, int l) { return l == 0 ? -O : -l; }
+__host__ __device__ constexpr int dhi(int O, int l) { return l == 0 ? O : O - l; }
 
-    const int64_t i = (int64_t)blockIdx.x * kStencilThreads + threadIdx.x;
-    if (i < t.n) {
-        const int64_t nxz = t.nx * t.nz;
-        const int64_t iy = i / nxz, r = i - iy * nxz, iz = r / t.nx, ix = r - iz * t.nx;
-        const float pc = a.cur[i];
-        const float q = a.prev[i];
-        float s = 1.f;
-        if (SPONGE) s = __ldg(a.sx + ix) * __ldg(a.sy + iy) * __ldg(a.sz + iz);
-        const float qd = SPONGE ? s * q : q;
-        float v = qd;
-        if (ix > 0 && ix < t.nx - 1 && iz > 0 && iz < t.nz - 1 && iy > 0 && iy < t.ny - 1) {
-            const int lx = (int)(ix % O), lz = (int)(iz % O), ly = (int)(iy % O);
-            const float *Tx = sT + lx * W, *Tz = sT + lz * W, *Ty = sT + ly * W;
-            float ax = 0.f, az = 0.f, ay = 0.f;
+template <int O>
+__device__ __forceinline__ void load_o(const float *p, float (&v)[O])
+{
+    if constexpr (O == 4) {
+        const float4 t = *reinterpret_cast<const float4 *>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else if constexpr (O == 2) {
+        const float2 t = *reinterpret_cast<const float2 *>(p);
+        v[0] = t.x; v[1] = t.y;
+    } else {
 #pragma unroll
-            for (int d = -O; d <= O; d++) {
-                if (d == 0) continue;
-                // offsets with a zero coefficient may leave the box: clamp them onto the axis
-                const int64_t dx = min(max((int64_t)d, -ix), t.nx - 1 - ix);
-                const int64_t dz = min(max((int64_t)d, -iz), t.nz - 1 - iz);
-                const int64_t dy = min(max((int64_t)d, -iy), t.ny - 1 - iy);
-                ax = fmaf(Tx[d + O], __ldg(a.cur + i + dx) - pc, ax);
-                az = fmaf(Tz[d + O], __ldg(a.cur + i + dz * t.nx) - pc, az);
-                ay = fmaf(Ty[d + O], __ldg(a.cur + i + dy * nxz) - pc, ay);
-            }
-            const float wx = sW[lx], wz = sW[lz], wy = sW[ly];
-            const float y = (t.g[0] * (wz * wy)) * ax + (t.g[1] * (wx * wy)) * az + (t.g[2] * (wx * wz)) * ay;
-            v = (2.f * pc - qd) - __ldg(a.a + i) * y;
-        }
-        a.prev[i] = SPONGE ? s * v : v;
-    }
-    if (a.nrec > 0) {
-        __shared__ int r_lo, r_hi;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const int64_t b0 = (int64_t)blockIdx.x * kStencilThreads;
-            int lo = 0, hi = a.nrec;
-            while (lo < hi) { int m = (lo + hi) >> 1; if (a.rec_node[m] < b0) lo = m + 1; else hi = m; }
-            r_lo = lo;
-            hi = a.nrec;
-            while (lo < hi) { int m = (lo + hi) >> 1; if (a.rec_node[m] < b0 + kStencilThreads) lo = m + 1; else hi = m; }
-            r_hi = lo;
-        }
-        __syncthreads();
-        const int step = a.ctr[1];
-        for (int rr = r_lo + threadIdx.x; rr < r_hi; rr += kStencilThreads)
-            a.traces[(int64_t)step * a.nrec + a.rec_perm[rr]] = a.prev[a.rec_node[rr]];
+        for (int j = 0; j < O; j++) v[j] = p[j];
     }
 }
 
 template <int O>
-cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, bool sponge, cudaStream_t s)
+struct VecO {
+    float v[O];
+};
+
+// Axis term along a direction whose local index LOC is uniform over the thread's O nodes:
+// r[j] = sum_d T[LOC][d] (row(d)[j] - c[j]).  row(d) returns the pointer to the O values at
+// offset d along the axis.
+template <int O, int LOC, class RowFn>
+__device__ __forceinline__ VecO<O> axis_uniform(const float (&c)[O], const RowFn &row)
 {
-    const int64_t grid = (t.n + kStencilThreads - 1) / kStencilThreads;
-    if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
-    if (sponge) k_stencil_simple<O, true><<<(unsigned)grid, kStencilThreads, 0, s>>>(t, a);
-    else k_stencil_simple<O, false><<<(unsigned)grid, kStencilThreads, 0, s>>>(t, a);
+    VecO<O> r;
+#pragma unroll
+    for (int j = 0; j < O; j++) r.v[j] = 0.f;
+#pragma unroll
+    for (int d = dlo(O, LOC); d <= dhi(O, LOC); d++) {
+        if (d == 0) continue;
+        float v[O];
+        load_o<O>(row(d), v);
+        const float t = c_T[O - 1][LOC * (2 * O + 1) + d + O];
+#pragma unroll
+        for (int j = 0; j < O; j++) r.v[j] = fmaf(t, v[j] - c[j], r.v[j]);
+    }
+    return r;
+}
+
+template <int O, class RowFn>
+__device__ __forceinline__ VecO<O> axis_dispatch(int loc, const float (&c)[O], const RowFn &row)
+{
+    switch (loc) {
+    case 0: return axis_uniform<O, 0>(c, row);
+    case 1: if constexpr (O > 1) return axis_uniform<O, 1>(c, row);
+    case 2: if constexpr (O > 2) return axis_uniform<O, 2>(c, row);
+    case 3: if constexpr (O > 3) return axis_uniform<O, 3>(c, row);
+    default: if constexpr (O > 4) return axis_uniform<O, 4>(c, row);
+    }
+    return axis_uniform<O, 0>(c, row);  // not reached: loc < O
+}
+
+// z-neighbour rows: ring slot rows are contiguous over the tile and its z halo.
+struct ZRows {
+    const float *base;  // current plane, row of the thread's node, first column of its nodes
+    int txp;
+    __device__ __forceinline__ const float *operator()(int d) const { return base + d * txp; }
+};
+
+// y-neighbour rows: ring slot of plane y+d (slot index of plane y is `slot`, ring of `r`).
+struct YPlanes {
+    const float *ring;
+    int slot, r, slot_floats, off;
+    __device__ __forceinline__ const float *operator()(int d) const
+    {
+        int i = slot + d;
+        if (d > 0) i = i >= r ? i - r : i;
+        if (d < 0) i = i < 0 ? i + r : i;
+        return ring + i * slot_floats + off;
+    }
+};
+
+template <int O, bool SPONGE>
+__global__ void __launch_bounds__(Cfg<O>::THREADS, 1)
+    k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap prev_map,
+              const __grid_constant__ CUtensorMap a_map, const StencilTables t, const StencilArgs a)
+{
+    using C = Cfg<O>;
+    constexpr int TZ = C::TZ, TX = C::TX, HX = C::HX, TXP = C::TXP, R = C::R, AUX = C::AUX;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float *ring = reinterpret_cast<float *>(smem);
+    float *aux = reinterpret_cast<float *>(smem + C::OFF_AUX);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + C::OFF_BAR);  // [R] ring, [AUX] aux
+    __shared__ int s_abort;
+
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
+    const int yb = blockIdx.z * t.ychunk;
+    const int ye = (int)min((int64_t)t.ny, (int64_t)yb + t.ychunk);
+    const int nx = (int)t.nx, nz = (int)t.nz, ny = (int)t.ny;
+
+    // ring plane p (p >= yb - O) lives in slot (p - yb + O) % R; aux plane p in (p - yb) % AUX
+    const CUtensorMap *rmap = &ring_map, *pmap = &prev_map, *amap = &a_map;  // parameter space
+    auto issue_ring = [=](int p) {
+        const int i = (p - yb + O) % R;
+        bar_arrive_expect_tx(bars + i, C::RING_TX);
+        tma_load_3d(ring + i * C::RING_FLOATS, rmap, x0 - HX, z0 - O, p, bars + i);
+    };
+    auto issue_aux = [=](int p) {
+        const int i = (p - yb) % AUX;
+        float *b = aux + i * C::AUX_FLOATS;
+        bar_arrive_expect_tx(bars + R + i, C::AUX_TX);
+        tma_load_3d(b, pmap, x0, z0, p, bars + R + i);
+        tma_load_3d(b + C::TILE_FLOATS, amap, x0, z0, p, bars + R + i);
+    };
+
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        for (int i = 0; i < R + AUX; i++) bar_init(bars + i, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int p = yb - O; p <= min(yb + O + kLook - 1, ye - 1 + O); p++) issue_ring(p);
+        for (int p = yb; p <= min(yb + kLook - 1, ye - 1); p++) issue_aux(p);
+    }
+
+    // per-thread constants
+    const int z = z0 + w;
+    const bool row_ok = z < nz;
+    const bool zin = z > 0 && z < nz - 1;
+    const int lz = z % O;
+    const int xb = x0 + O * l;  // first node of the thread
+    float sxv[O];
+#pragma unroll
+    for (int j = 0; j < O; j++) sxv[j] = (SPONGE && xb + j < nx) ? __ldg(a.sx + xb + j) : 1.f;
+    const float szv = (SPONGE && row_ok) ? __ldg(a.sz + z) : 1.f;
+    const float wz = c_wa[O - 1][lz];
+    const int off = (w + O) * TXP + HX + O * l;  // in-slot offset of the thread's first node
+    const int toff = w * TX + O * l;             // in-tile offset (aux tiles)
+    float *dst_col = a.prev + (int64_t)xb + (int64_t)z * t.nxp;
+    const int64_t plane_stride = t.nxp * t.nz;
+
+    bool ok = true;
+    for (int p = yb - O; p < yb + O; p++) {
+        const int i = p - yb + O;  // < 2O < R: first fill of each of these slots
+        ok &= bar_wait(bars + i, 0, kWaitLimitNs);
+    }
+    if (!ok) { s_abort = 1; atomicExch(a.status, 1); }
+
+    int rs = O;     // ring slot of plane y
+    int as = 0;     // aux slot of plane y
+    int ly = yb % O;
+    for (int y = yb; y < ye; y++) {
+        if (threadIdx.x == 0 && y + kLook <= ye - 1) {
+            issue_ring(y + O + kLook);
+            issue_aux(y + kLook);
+        }
+        {
+            const int pr = y + O - yb + O;  // fill index of ring plane y+O
+            const int pa = y - yb;
+            ok = bar_wait(bars + pr % R, (uint32_t)((pr / R) & 1), kWaitLimitNs);
+            ok &= bar_wait(bars + R + as, (uint32_t)((pa / AUX) & 1), kWaitLimitNs);
+            if (!ok) { s_abort = 1; atomicExch(a.status, 1); }
+        }
+        if (row_ok) {
+            const float *cur = ring + rs * C::RING_FLOATS + off;
+            const float *tq = aux + as * C::AUX_FLOATS + toff;
+            float c[O], left[O], q[O], am[O];
+            load_o<O>(cur, c);
+            load_o<O>(cur - O, left);
+            const float right = cur[O];
+            load_o<O>(tq, q);
+            load_o<O>(tq + C::TILE_FLOATS, am);
+
+            // x: local index j is compile-time
+            float ax[O];
+#pragma unroll
+            for (int j = 0; j < O; j++) {
+                float acc = 0.f;
+#pragma unroll
+                for (int d = dlo(O, j); d <= dhi(O, j); d++) {
+                    if (d == 0) continue;
+                    const int m = j + d;  // offset from the thread's first node, in [-O, O]
+                    const float v = m < 0 ? left[m + O] : (m < O ? c[m] : right);
+                    acc = fmaf(c_T[O - 1][j * (2 * O + 1) + d + O], v - c[j], acc);
+                }
+                ax[j] = acc;
+            }
+            const VecO<O> az = axis_dispatch<O>(lz, c, ZRows{cur, TXP});
+            const VecO<O> ay = axis_dispatch<O>(ly, c, YPlanes{ring, rs, R, C::RING_FLOATS, off});
+
+            const bool yin = y > 0 && y < ny - 1;
+            const float wy = c_wa[O - 1][ly];
+            const float syv = SPONGE ? __ldg(a.sy + y) : 1.f;
+            const float gx = t.g[0] * (wz * wy), gzy = t.g[1] * wy, gyz = t.g[2] * wz;
+            float out[O];
+#pragma unroll
+            for (int j = 0; j < O; j++) {
+                const float wxj = c_wa[O - 1][j];
+                const float s = SPONGE ? sxv[j] * syv * szv : 1.f;  // (sx*sy)*sz
+                const float qd = SPONGE ? s * q[j] : q[j];
+                float v = qd;
+                if (xb + j > 0 && xb + j < nx - 1 && zin && yin) {
+                    const float yv = gx * ax[j] + (gzy * wxj) * az.v[j] + (gyz * wxj) * ay.v[j];
+                    v = (2.f * c[j] - qd) - am[j] * yv;
+                }
+                out[j] = xb + j < nx ? (SPONGE ? s * v : v) : 0.f;
+            }
+            float *dst = dst_col + (int64_t)y * plane_stride;
+            if constexpr (O == 4) {
+                if (xb + 4 <= t.nxp) *reinterpret_cast<float4 *>(dst) = make_float4(out[0], out[1], out[2], out[3]);
+            } else if constexpr (O == 2) {
+                if (xb + 2 <= t.nxp) *reinterpret_cast<float2 *>(dst) = make_float2(out[0], out[1]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < O; j++)
+                    if (xb + j < t.nxp) dst[j] = out[j];
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+        rs = rs + 1 == R ? 0 : rs + 1;
+        as = as + 1 == AUX ? 0 : as + 1;
+        ly = ly + 1 == O ? 0 : ly + 1;
+    }
+
+    if (s_abort) {
+        // leave no copy in flight into this CTA's shared memory: bounded drain of every barrier
+        if (threadIdx.x == 0)
+            for (int i = 0; i < R + AUX; i++) {
+                bar_wait(bars + i, 0, kWaitLimitNs / 8);
+                bar_wait(bars + i, 1, kWaitLimitNs / 8);
+            }
+        return;
+    }
+    if (a.nrec > 0) {
+        const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        const int r0 = a.rec_off[cta], r1 = a.rec_off[cta + 1];
+        if (r0 < r1) {  // uniform over the CTA; its new values are visible after the last barrier
+            const int step = a.ctr[1];
+            for (int r = r0 + threadIdx.x; r < r1; r += C::THREADS) {
+                const int j = a.rec_idx[r];
+                a.traces[(int64_t)step * a.nrec + a.rec_perm[j]] = a.prev[a.rec_node[j]];
+            }
+        }
+    }
+}
+
+template <int O>
+size_t smem_of() { return Cfg<O>::SMEM; }
+
+size_t smem_bytes(int order)
+{
+    switch (order) {
+    case 1: return smem_of<1>();
+    case 2: return smem_of<2>();
+    case 3: return smem_of<3>();
+    case 4: return smem_of<4>();
+    default: return smem_of<5>();
+    }
+}
+
+template <int O>
+void tile_of(int &tx, int &tz, int &hx) { tx = Cfg<O>::TX; tz = Cfg<O>::TZ; hx = Cfg<O>::HX; }
+
+void tile_dims(int order, int &tx, int &tz, int &hx)
+{
+    switch (order) {
+    case 1: tile_of<1>(tx, tz, hx); break;
+    case 2: tile_of<2>(tx, tz, hx); break;
+    case 3: tile_of<3>(tx, tz, hx); break;
+    case 4: tile_of<4>(tx, tz, hx); break;
+    default: tile_of<5>(tx, tz, hx); break;
+    }
+}
+
+template <int O>
+cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, cudaStream_t s)
+{
+    const dim3 grid(t.grid[0], t.grid[1], t.grid[2]);
+    const LevelMaps &cm = t.lv[ci], &pm = t.lv[1 - ci];
+    if (sponge)
+        k_stencil<O, true><<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.ring, pm.tile, t.amap, t, a);
+    else
+        k_stencil<O, false><<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.ring, pm.tile, t.amap, t, a);
     return cudaGetLastError();
+}
+
+template <int O>
+cudaError_t setup_o()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_stencil<O, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<O>::SMEM);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_stencil<O, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<O>::SMEM);
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder()
+{
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+// 3-D map over the device layout (nxp, nz, ny) of float buffer `base` with box (bx, bz, 1).
+bool make_map(CUtensorMap &m, const float *base, const StencilTables &t, int bx, int bz)
+{
+    EncodeTiled enc = encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)t.nxp, (cuuint64_t)t.nz, (cuuint64_t)t.ny};
+    const cuuint64_t strides[2] = {(cuuint64_t)t.nxp * 4, (cuuint64_t)t.nxp * t.nz * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)bz, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace
@@ -123,15 +415,83 @@ int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, Stenc
 {
     StencilTables *t = new StencilTables();
     t->order = b.order;
-    t->nx = b.nx; t->ny = b.ny; t->nz = b.nz; t->n = b.n_nodes;
+    t->nx = b.nx; t->nxp = b.nxp; t->ny = b.ny; t->nz = b.nz;
     for (int d = 0; d < 3; d++) t->g[d] = (float)geo.g[d];
     for (int l = 0; l < b.order; l++) t->wa[l] = (float)(l == 0 ? g.w[0] + g.w[b.order] : g.w[l]);
+    tile_dims(b.order, t->tile_x, t->tile_z, t->halo_x);
+    t->smem = smem_bytes(b.order);
+    t->grid[0] = (int)((b.nx + t->tile_x - 1) / t->tile_x);
+    t->grid[1] = (int)((b.nz + t->tile_z - 1) / t->tile_z);
+    // y-chunking: balance the last wave against the 2o warm-up planes of every chunk
+    int dev = 0, sms = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    per_sm = std::max(1, std::min(2048 / (32 * t->tile_z), smem_sm / (int)(t->smem + 1024)));
+    const int64_t cols = (int64_t)t->grid[0] * t->grid[1];
+    const int64_t resident = (int64_t)sms * per_sm;
+    double best = 1e300;
+    int best_c = 1;
+    for (int c = 1; c <= 64 && c <= b.ny; c++) {
+        const int64_t chunk = (b.ny + c - 1) / c;
+        const int64_t waves = (cols * c + resident - 1) / resident;
+        const double cost = (double)waves * (chunk + 2 * b.order);
+        if (cost < best - 1e-9) { best = cost; best_c = c; }
+    }
+    t->ychunk = (int)((b.ny + best_c - 1) / best_c);
+    t->grid[2] = (int)((b.ny + t->ychunk - 1) / t->ychunk);
     *out = t;
     return 0;
 }
 
+int stencil_bind(StencilTables &t, const float *p0, const float *p1, const float *a)
+{
+    if (t.bound[0] == p0 && t.bound[1] == p1 && t.bound[2] == a) return 0;
+    const int txp = t.tile_x + 2 * t.halo_x;
+    const float *ps[2] = {p0, p1};
+    for (int i = 0; i < 2; i++) {
+        if (!make_map(t.lv[i].ring, ps[i], t, txp, t.tile_z + 2 * t.order) ||
+            !make_map(t.lv[i].tile, ps[i], t, t.tile_x, t.tile_z))
+            return (int)cudaErrorInvalidValue;
+    }
+    if (!make_map(t.amap, a, t, t.tile_x, t.tile_z)) return (int)cudaErrorInvalidValue;
+    t.bound[0] = p0; t.bound[1] = p1; t.bound[2] = a;
+    return 0;
+}
+
+cudaError_t stencil_set_receivers(StencilTables &t, const int64_t *sorted_nodes, int nrec, uint64_t version)
+{
+    if (t.d_rec_off) { cudaFree(t.d_rec_off); t.d_rec_off = nullptr; }
+    if (t.d_rec_idx) { cudaFree(t.d_rec_idx); t.d_rec_idx = nullptr; }
+    t.rec_version = version;
+    if (nrec <= 0) return cudaSuccess;
+    const int64_t ncta = (int64_t)t.grid[0] * t.grid[1] * t.grid[2];
+    std::vector<int64_t> owner(nrec);
+    std::vector<int> count(ncta + 1, 0);
+    const int64_t nxz = t.nxp * t.nz;
+    for (int r = 0; r < nrec; r++) {
+        const int64_t n = sorted_nodes[r];
+        const int64_t y = n / nxz, rem = n - y * nxz, z = rem / t.nxp, x = rem - z * t.nxp;
+        owner[r] = x / t.tile_x + t.grid[0] * (z / t.tile_z + t.grid[1] * (y / t.ychunk));
+        count[owner[r] + 1]++;
+    }
+    for (int64_t c = 0; c < ncta; c++) count[c + 1] += count[c];
+    std::vector<int> idx(nrec), fill(count.begin(), count.end() - 1);
+    for (int r = 0; r < nrec; r++) idx[fill[owner[r]]++] = r;
+    cudaError_t e;
+    if ((e = cudaMalloc(&t.d_rec_off, (ncta + 1) * sizeof(int))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&t.d_rec_idx, nrec * sizeof(int))) != cudaSuccess) return e;
+    if ((e = cudaMemcpy(t.d_rec_off, count.data(), (ncta + 1) * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return e;
+    return cudaMemcpy(t.d_rec_idx, idx.data(), nrec * sizeof(int), cudaMemcpyHostToDevice);
+}
+
 void stencil_tables_free(StencilTables *&t)
 {
+    if (!t) return;
+    if (t->d_rec_off) cudaFree(t->d_rec_off);
+    if (t->d_rec_idx) cudaFree(t->d_rec_idx);
     delete t;
     t = nullptr;
 }
@@ -144,25 +504,32 @@ cudaError_t stencil_kernel_setup()
     if (e != cudaSuccess) return e;
     for (int d : done_devices)
         if (d == dev) return cudaSuccess;
-    std::vector<float> all(kMaxOrder * kTMax, 0.f);
+    std::vector<float> all(kMaxOrder * kTMax, 0.f), wa(kMaxOrder * kMaxOrder, 0.f);
     for (int o = 1; o <= kMaxOrder; o++) {
         Gll g;
         gll_tables(o, g);
         build_T(g, all.data() + (o - 1) * kTMax);
+        for (int l = 0; l < o; l++) wa[(o - 1) * kMaxOrder + l] = (float)(l == 0 ? g.w[0] + g.w[o] : g.w[l]);
     }
-    e = cudaMemcpyToSymbol(c_T, all.data(), all.size() * sizeof(float));
-    if (e == cudaSuccess) done_devices.push_back(dev);
-    return e;
+    if ((e = cudaMemcpyToSymbol(c_T, all.data(), all.size() * sizeof(float))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_wa, wa.data(), wa.size() * sizeof(float))) != cudaSuccess) return e;
+    if ((e = setup_o<1>()) != cudaSuccess) return e;
+    if ((e = setup_o<2>()) != cudaSuccess) return e;
+    if ((e = setup_o<3>()) != cudaSuccess) return e;
+    if ((e = setup_o<4>()) != cudaSuccess) return e;
+    if ((e = setup_o<5>()) != cudaSuccess) return e;
+    done_devices.push_back(dev);
+    return cudaSuccess;
 }
 
-cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, bool sponge, cudaStream_t s)
+cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, int cur_index, bool sponge, cudaStream_t s)
 {
     switch (t.order) {
-    case 1: return launch_o<1>(t, a, sponge, s);
-    case 2: return launch_o<2>(t, a, sponge, s);
-    case 3: return launch_o<3>(t, a, sponge, s);
-    case 4: return launch_o<4>(t, a, sponge, s);
-    case 5: return launch_o<5>(t, a, sponge, s);
+    case 1: return launch_o<1>(t, a, cur_index, sponge, s);
+    case 2: return launch_o<2>(t, a, cur_index, sponge, s);
+    case 3: return launch_o<3>(t, a, cur_index, sponge, s);
+    case 4: return launch_o<4>(t, a, cur_index, sponge, s);
+    case 5: return launch_o<5>(t, a, cur_index, sponge, s);
     default: return cudaErrorInvalidValue;
     }
 }

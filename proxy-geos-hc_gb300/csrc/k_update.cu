@@ -1,4 +1,4 @@
-// k_update.cu -- node-wise kernels of the SEM step and its set-up.
+// k_update.cu -- node-wise kernels of the SEM step and its set-up (device layout of kernels.h).
 //
 //  k_source   SEMsolver.cpp:39-43    p^n[node0(e_k)] += dt^2 c_e^2 r_k(t_n), sources in order
 //  k_update   SEMsolver.cpp:85-89    p^{n+1} = 2 p^n - p^{n-1} - dt^2 y / M on interior nodes,
@@ -25,72 +25,53 @@ __global__ void k_source(const SourceArgs a)
     a.ctr[0] = n + 1;
 }
 
-__device__ __forceinline__ int lower_bound64(const int64_t *v, int n, int64_t key)
-{
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (v[mid] < key) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
 template <bool SPONGE>
 __global__ void __launch_bounds__(kUpdateThreads) k_update(const UpdateArgs a)
 {
     constexpr int V = kUpdateNodesPerThread;
     const int64_t i0 = ((int64_t)blockIdx.x * kUpdateThreads + threadIdx.x) * V;
-    if (i0 < a.n) {
-        const int64_t nxz = a.nx * a.nz;
-        int64_t iy = i0 / nxz;
-        const int64_t r = i0 - iy * nxz;
-        int64_t iz = r / a.nx;
-        int64_t ix = r - iz * a.nx;
-        // arrays are padded to a multiple of 4 floats, so these vector accesses stay in bounds
+    if (i0 < a.n_int) {
+        // rows are padded to a multiple of 4 nodes: the 4 nodes share one row
+        const int64_t nxz = a.nxp * a.nz;
+        const int64_t iy = i0 / nxz, r = i0 - iy * nxz, iz = r / a.nxp, ix0 = r - iz * a.nxp;
         const float4 c4 = *reinterpret_cast<const float4 *>(a.cur + i0);
         const float4 q4 = *reinterpret_cast<const float4 *>(a.prev + i0);
         const float4 y4 = *reinterpret_cast<const float4 *>(a.y + i0);
         const float4 a4 = __ldg(reinterpret_cast<const float4 *>(a.a + i0));
         const float cc[V] = {c4.x, c4.y, c4.z, c4.w}, qq[V] = {q4.x, q4.y, q4.z, q4.w};
         const float yy[V] = {y4.x, y4.y, y4.z, y4.w}, aa[V] = {a4.x, a4.y, a4.z, a4.w};
+        const bool zy_in = iz > 0 && iz < a.nz - 1 && iy > 0 && iy < a.ny - 1;
+        float syz = 1.f, szv = 1.f;
+        if (SPONGE && ix0 < a.nx) { syz = __ldg(a.sy + iy); szv = __ldg(a.sz + iz); }
         float out[V];
 #pragma unroll
         for (int t = 0; t < V; t++) {
-            out[t] = 0.f;
-            if (i0 + t < a.n) {
+            const int64_t ix = ix0 + t;
+            out[t] = 0.f;  // padding stays zero
+            if (ix < a.nx) {
                 float s = 1.f;
-                if (SPONGE) s = __ldg(a.sx + ix) * __ldg(a.sy + iy) * __ldg(a.sz + iz);
+                if (SPONGE) s = __ldg(a.sx + ix) * syz * szv;  // (sx*sy)*sz
                 const float qd = SPONGE ? s * qq[t] : qq[t];
-                const bool interior = ix > 0 && ix < a.nx - 1 && iz > 0 && iz < a.nz - 1 &&
-                                      iy > 0 && iy < a.ny - 1;
+                const bool interior = zy_in && ix > 0 && ix < a.nx - 1;
                 const float v = interior ? (2.f * cc[t] - qd) - aa[t] * yy[t] : qd;
                 out[t] = SPONGE ? s * v : v;
-                if (++ix == a.nx) {
-                    ix = 0;
-                    if (++iz == a.nz) { iz = 0; ++iy; }
-                }
             }
         }
         *reinterpret_cast<float4 *>(a.prev + i0) = make_float4(out[0], out[1], out[2], out[3]);
         *reinterpret_cast<float4 *>(a.y + i0) = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (a.nrec > 0) {
-        __shared__ int r_lo, r_hi;
-        __syncthreads();  // this block's new values are visible to the whole block
-        if (threadIdx.x == 0) {
-            const int64_t b0 = (int64_t)blockIdx.x * kUpdateThreads * V;
-            r_lo = lower_bound64(a.rec_node, a.nrec, b0);
-            r_hi = lower_bound64(a.rec_node, a.nrec, b0 + (int64_t)kUpdateThreads * V);
+        const int r0 = a.rec_off[blockIdx.x], r1 = a.rec_off[blockIdx.x + 1];
+        if (r0 < r1) {  // uniform over the block
+            __syncthreads();  // this block's new values are visible to the whole block
+            const int step = a.ctr[1];
+            for (int r = r0 + threadIdx.x; r < r1; r += kUpdateThreads)
+                a.traces[(int64_t)step * a.nrec + a.rec_perm[r]] = a.prev[a.rec_node[r]];
         }
-        __syncthreads();
-        const int step = a.ctr[1];
-        for (int r = r_lo + threadIdx.x; r < r_hi; r += kUpdateThreads)
-            a.traces[(int64_t)step * a.nrec + a.rec_perm[r]] = a.prev[a.rec_node[r]];
     }
 }
 
-__global__ void k_connectivity(int32_t *conn, int ex, int ez, int order, int64_t nx, int64_t nz,
+__global__ void k_connectivity(int32_t *conn, int ex, int ez, int order, int64_t nxp, int64_t nz,
                                int64_t n_elem)
 {
     const int o1 = order + 1, npe = o1 * o1 * o1;
@@ -101,7 +82,7 @@ __global__ void k_connectivity(int32_t *conn, int ex, int ez, int order, int64_t
         const int loc = (int)(q - e * npe);
         const int64_t ix = e % ex, iz = (e / ex) % ez, iy = e / ((int64_t)ex * ez);
         const int l = loc % o1, n = (loc / o1) % o1, m = loc / (o1 * o1);
-        conn[q] = (int32_t)((ix * order + l) + (iz * order + n) * nx + (iy * order + m) * nx * nz);
+        conn[q] = (int32_t)((ix * order + l) + (iz * order + n) * nxp + (iy * order + m) * nxp * nz);
     }
 }
 
@@ -118,13 +99,17 @@ __device__ __forceinline__ void adj_range(int64_t i, int order, int ne, int64_t 
 }
 
 __global__ void k_mass(float *a, const float *vel, const float *slow2, int ex, int ey, int ez,
-                       int order, const double *w, double detJ, double dt2)
+                       int order, int64_t nxp, const double *w, double detJ, double dt2)
 {
     const int64_t nx = (int64_t)ex * order + 1, ny = (int64_t)ey * order + 1,
-                  nz = (int64_t)ez * order + 1, n = nx * ny * nz;
+                  nz = (int64_t)ez * order + 1, n = nxp * ny * nz;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t iy = q / (nx * nz), r = q - iy * nx * nz, iz = r / nx, ix = r - iz * nx;
+        const int64_t iy = q / (nxp * nz), r = q - iy * nxp * nz, iz = r / nxp, ix = r - iz * nxp;
+        if (ix >= nx) {
+            a[q] = 0.f;
+            continue;
+        }
         // local weight of the node: w[i mod o] (element-boundary nodes have w_0 = w_o)
         const double wq = w[ix % order] * w[iz % order] * w[iy % order];
         int64_t x0, x1, z0, z1, y0, y1;
@@ -153,8 +138,8 @@ __global__ void k_mass(float *a, const float *vel, const float *slow2, int ex, i
 
 cudaError_t launch_update(const UpdateArgs &a, bool sponge, cudaStream_t s)
 {
-    if (a.n <= 0) return cudaSuccess;
-    const int64_t grid = update_grid(a.n);
+    if (a.n_int <= 0) return cudaSuccess;
+    const int64_t grid = update_grid(a.n_int);
     if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
     if (sponge) k_update<true><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
     else k_update<false><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
@@ -167,18 +152,20 @@ cudaError_t launch_source(const SourceArgs &a, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_connectivity(int32_t *conn, int ex, int ey, int ez, int order, cudaStream_t s)
+cudaError_t launch_connectivity(int32_t *conn, int ex, int ey, int ez, int order, int64_t nxp,
+                                cudaStream_t s)
 {
-    const int64_t nx = (int64_t)ex * order + 1, nz = (int64_t)ez * order + 1;
+    const int64_t nz = (int64_t)ez * order + 1;
     const int64_t ne = (int64_t)ex * ey * ez;
-    k_connectivity<<<152 * 16, 256, 0, s>>>(conn, ex, ez, order, nx, nz, ne);
+    k_connectivity<<<152 * 16, 256, 0, s>>>(conn, ex, ez, order, nxp, nz, ne);
     return cudaGetLastError();
 }
 
 cudaError_t launch_mass(float *a, const float *vel, const float *slow2, int ex, int ey, int ez,
-                        int order, const double *w_dev, double detJ, double dt2, cudaStream_t s)
+                        int order, int64_t nxp, const double *w_dev, double detJ, double dt2,
+                        cudaStream_t s)
 {
-    k_mass<<<152 * 16, 256, 0, s>>>(a, vel, slow2, ex, ey, ez, order, w_dev, detJ, dt2);
+    k_mass<<<152 * 16, 256, 0, s>>>(a, vel, slow2, ex, ey, ez, order, nxp, w_dev, detJ, dt2);
     return cudaGetLastError();
 }
 

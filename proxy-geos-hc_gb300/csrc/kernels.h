@@ -1,10 +1,11 @@
-// kernels.h -- launch interface between the C ABI (api.cu) and the device kernels.
+// kernels.h -- launch interface between the C ABI (api.cu) and the element-path kernels.
 //
-// Data layout in HBM (reference node numbering, node = ix + iz*nx + iy*nx*nz):
-//   p[2][N4]   float   the two pressure levels (N4 = N rounded up to 4, zero tail)
-//   y[N4]      float   K.p accumulator of the element path (scratch, zero between steps)
-//   a[N4]      float   dt^2 / M_i (mass with the velocity model folded in)
-//   conn[NE][(o+1)^3] int32  element-to-node map (element path only)
+// Data layout in HBM (device layout of host_util.h: rows along x padded to nxp, node index
+// q = ix + iz*nxp + iy*nxp*nz, padding nodes zero):
+//   p[2][n_int]   float   the two pressure levels
+//   y[n_int]      float   K.p accumulator of the element path (scratch, zero between steps)
+//   a[n_int]      float   dt^2 / M_i (mass with the velocity model folded in)
+//   conn[NE][(o+1)^3] int32  element-to-node map in device-layout indices (element path)
 //   sx[nx], sy[ny], sz[nz]   float  sponge factors per axis
 // The level that a step reads as "previous" is stored without its last sponge factor; the
 // step applies s_i when it reads it (fl(s_i * p) is the value the reference would have stored).
@@ -39,14 +40,14 @@ struct ElementArgs {
 struct UpdateArgs {
     const float *cur;
     float *prev;         // in: stored previous level; out: new level
-    float *y;            // read then zeroed (element path)
+    float *y;            // read then zeroed
     const float *a;      // dt^2/M
     const float *sx, *sy, *sz;
-    int64_t nx, ny, nz, n;
-    // receivers (sorted by node within each block's node range)
-    const int64_t *rec_node;
+    int64_t nx, nxp, ny, nz, n_int;
+    // receivers, node-sorted, grouped by update block: rec_off[b]..rec_off[b+1]
+    const int64_t *rec_node;   // device-layout indices
     const int *rec_perm;
-    const int *rec_off;  // [grid+1]
+    const int *rec_off;
     int nrec;
     float *traces;       // [step][nrec]
     const int *ctr;      // ctr[1] = index of the step being run
@@ -54,7 +55,7 @@ struct UpdateArgs {
 
 struct SourceArgs {
     float *cur;
-    const int64_t *node;
+    const int64_t *node;   // device-layout indices
     const float *coef;     // dt^2 c_e^2 per source, rounded as the reference does
     const float *wavelet;  // [nsrc][nsamples]
     int nsrc, nsamples;
@@ -63,19 +64,19 @@ struct SourceArgs {
 
 constexpr int kUpdateThreads = 256;
 constexpr int kUpdateNodesPerThread = 4;
-inline int64_t update_grid(int64_t n)
-{
-    const int64_t per = (int64_t)kUpdateThreads * kUpdateNodesPerThread;
-    return (n + per - 1) / per;
-}
+constexpr int64_t kUpdateNodesPerBlock = (int64_t)kUpdateThreads * kUpdateNodesPerThread;
+inline int64_t update_grid(int64_t n) { return (n + kUpdateNodesPerBlock - 1) / kUpdateNodesPerBlock; }
 
 cudaError_t launch_element(int order, const ElementArgs &a, cudaStream_t s);
 cudaError_t launch_update(const UpdateArgs &a, bool sponge, cudaStream_t s);
 cudaError_t launch_source(const SourceArgs &a, cudaStream_t s);
-cudaError_t launch_connectivity(int32_t *conn, int ex, int ey, int ez, int order, cudaStream_t s);
-// a_i = dt^2 / M_i from per-element velocity (vel) or per-node squared slowness (slow2).
+cudaError_t launch_connectivity(int32_t *conn, int ex, int ey, int ez, int order, int64_t nxp,
+                                cudaStream_t s);
+// a_i = dt^2 / M_i from per-element velocity (vel) or per-node squared slowness (slow2, device
+// layout); zero on padding nodes.
 cudaError_t launch_mass(float *a, const float *vel, const float *slow2, int ex, int ey, int ez,
-                        int order, const double *w_dev, double detJ, double dt2, cudaStream_t s);
+                        int order, int64_t nxp, const double *w_dev, double detJ, double dt2,
+                        cudaStream_t s);
 cudaError_t element_kernel_setup();
 
 }  // namespace semgb

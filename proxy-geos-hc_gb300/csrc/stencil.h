@@ -11,6 +11,7 @@
 // sampling happen in the same pass (SEMsolver.cpp:85-89).
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "host_util.h"
@@ -18,28 +19,55 @@
 
 namespace semgb {
 
+// Tensor maps of one pressure buffer (3-D tiles of the device layout).
+struct LevelMaps {
+    CUtensorMap ring;   // (tile width + x halo) x (TZ + 2o rows) x 1 plane
+    CUtensorMap tile;   // tile width x TZ rows x 1 plane
+};
+
 struct StencilTables {
     int order = 0;
-    int64_t nx = 0, ny = 0, nz = 0, n = 0;
+    int64_t nx = 0, nxp = 0, ny = 0, nz = 0;
     float g[3] = {0, 0, 0};   // g_d = |detJ| / J_dd^2 for x (xi1), z (xi2), y (xi3)
     float wa[6] = {0};        // assembled weight by local index: wa[0] = 2 w_0, wa[l] = w_l
+    int tile_x = 0, tile_z = 0, halo_x = 0;
+    int grid[3] = {0, 0, 0};  // CTAs along x, z, y
+    int ychunk = 0;           // planes per CTA
+    size_t smem = 0;          // dynamic shared memory per CTA
+    LevelMaps lv[2];          // per pressure buffer
+    CUtensorMap amap;         // dt^2/M, tile boxes
+    const float *bound[3] = {nullptr, nullptr, nullptr};  // buffers the maps describe
+    // receivers grouped by the CTA that owns their node: rec_off[cta]..rec_off[cta+1] index
+    // rec_idx, which holds positions in the solver's node-sorted receiver arrays
+    int *d_rec_off = nullptr;
+    int *d_rec_idx = nullptr;
+    uint64_t rec_version = 0;
 };
 
 struct StencilArgs {
     const float *cur;
     float *prev;               // in: stored previous level; out: new level
-    const float *a;            // dt^2 / M
     const float *sx, *sy, *sz;
-    const int64_t *rec_node;
+    const int64_t *rec_node;   // node-sorted receivers (device-layout indices)
     const int *rec_perm;
+    const int *rec_off;        // per CTA (from StencilTables)
+    const int *rec_idx;
     int nrec;
     float *traces;
     const int *ctr;
+    int *status;               // set non-zero when a bounded wait gives up
 };
 
+// Tables and tiling for a box (no device buffers yet).  Returns 0 or a cudaError_t.
 int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, StencilTables **out);
+// Describe the solver's two pressure buffers and its dt^2/M buffer with tensor maps.
+int stencil_bind(StencilTables &t, const float *p0, const float *p1, const float *a);
+// Group node-sorted receivers (device-layout indices) by owning CTA (device CSR in t).
+cudaError_t stencil_set_receivers(StencilTables &t, const int64_t *sorted_nodes, int nrec, uint64_t version);
 void stencil_tables_free(StencilTables *&t);
 cudaError_t stencil_kernel_setup();
-cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, bool sponge, cudaStream_t s);
+// cur_index: which of the bound pressure buffers is the current level.
+cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, int cur_index, bool sponge,
+                           cudaStream_t s);
 
 }  // namespace semgb
