@@ -198,6 +198,31 @@ int sem_solver_synchronize(sem_solver *s);
  * Advances the solver by n_steps. */
 int sem_solver_time_kernels(sem_solver *s, int n_steps, float *ms);
 
+/* ------------------------------------------------------------------------------------------
+ * Allocation-free step.  This entry point has no counterpart in the reference.
+ * ------------------------------------------------------------------------------------------ */
+
+/* One element-path step (K.p by the element kernel, then the leapfrog update) on buffers the
+ * caller owns, for callers that cannot allocate device memory while they step -- a host code
+ * that gives all device memory to its own pool manager, or one whose time loop runs where
+ * allocation is not allowed.  The call allocates nothing: the K.p accumulator and a small
+ * coefficient table live in a fixed array of 4,194,304 floats (16 MiB) in the library's device
+ * image, so the mesh may have at most 4,194,176 nodes; larger meshes are rejected with
+ * SEM_ERR_ARG.  All buffers are device memory in the reference node numbering:
+ *   conn    int32 [n_elem][(order+1)^3] element-to-node map (as sem_mesh_get_connectivity gives)
+ *   p_cur   current level; sponge-damped in place when sponge factors are given
+ *   p_prev  previous level (already damped); replaced by the new level
+ *   coef    dt^2 / M_i per node
+ *   sx, sy, sz  per-axis sponge factors (sem_box_sponge_profile), or all three NULL
+ * Sources are the caller's: add them to p_cur before the call.  Work is enqueued on `stream`
+ * (a cudaStream_t; NULL is the legacy default stream).  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) and caches it; make that first call before
+ * any stream capture.  Every call uses the same array, which keeps the last call's contents
+ * (the call clears what it needs): calls whose work overlaps on the GPU race on it. */
+int sem_element_step_noalloc(int ex, int ey, int ez, float lx, float ly, float lz, int order,
+                             const int32_t *conn, float *p_cur, float *p_prev, const float *coef,
+                             const float *sx, const float *sy, const float *sz, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,11 @@ static int fail(int code, const std::string &msg)
     return code;
 }
 
+namespace semgb {
+// Sets the message sem_last_error_string() returns (for entry points defined in other files).
+void set_last_error(const std::string &msg) { g_err = msg; }
+}  // namespace semgb
+
 #define CUDA_TRY(call)                                                                       \
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \

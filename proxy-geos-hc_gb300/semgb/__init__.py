@@ -70,6 +70,7 @@ _SIGS = {
     "sem_solver_reset": [_VP],
     "sem_solver_synchronize": [_VP],
     "sem_solver_time_kernels": [_VP, C.c_int, _F32P],
+    "sem_element_step_noalloc": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int] + [_VP] * 8,
 }
 _RESTYPE = {"sem_last_error_string": C.c_char_p}
 
