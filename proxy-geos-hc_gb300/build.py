@@ -31,8 +31,11 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+_DEFINES: list[str] = []
+
+
 def _flags(src: str) -> list[str]:
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"), *_DEFINES]
     if src.endswith(".cu"):
         return common + ARCH + ["-lineinfo", "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
     return common + ["-x", "c++"]
@@ -59,11 +62,19 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, defines: list[str] | None = None,
+          out: str | None = None) -> str:
+    """Build libsemgb.so (into `out` if given; `defines` are extra -D macros for the CUDA units)."""
+    global LIB, BUILD_DIR
+    if out or defines:
+        LIB = out or LIB
+        BUILD_DIR = os.path.join(os.path.dirname(LIB), "_build")
+        _DEFINES[:] = [f"-D{d}" for d in (defines or [])]
+        force = True
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD_DIR, exist_ok=True)
-    os.makedirs(OUT_DIR, exist_ok=True)
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     tmp = LIB + ".tmp"
@@ -76,4 +87,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("-v", action="store_true")
+    ap.add_argument("-D", action="append", default=[], help="extra macro for the CUDA units")
+    ap.add_argument("--out", default=None, help="output path of the library")
+    a = ap.parse_args()
+    print(build(force=a.force, verbose=a.v, defines=a.D, out=a.out))

@@ -31,7 +31,13 @@ namespace semgb {
 
 namespace {
 
-constexpr int kLook = 2;                   // planes of lookahead
+#ifndef SEM_STENCIL_LOOKAHEAD
+#define SEM_STENCIL_LOOKAHEAD 1
+#endif
+#ifndef SEM_STENCIL_ROWS
+#define SEM_STENCIL_ROWS 8
+#endif
+constexpr int kLook = SEM_STENCIL_LOOKAHEAD;  // planes of lookahead
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 constexpr int kTMax = kMaxOrder * (2 * kMaxOrder + 1);
 __constant__ float c_T[kMaxOrder][kTMax];  // [order-1][l * (2o+1) + d + o]
@@ -39,7 +45,7 @@ __constant__ float c_wa[kMaxOrder][kMaxOrder];  // assembled weights by local in
 
 template <int O>
 struct Cfg {
-    static constexpr int TZ = O == 5 ? 8 : 16;          // rows (warps) per CTA
+    static constexpr int TZ = O == 5 ? 8 : SEM_STENCIL_ROWS;  // rows (warps) per CTA
     static constexpr int THREADS = 32 * TZ;
     static constexpr int TX = 32 * O;                   // nodes along x per CTA
     static constexpr int HX = O <= 4 ? 4 : 8;           // x halo, a multiple of 4 floats
@@ -164,7 +170,7 @@ struct YPlanes {
 };
 
 template <int O, bool SPONGE>
-__global__ void __launch_bounds__(Cfg<O>::THREADS, 1)
+__global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::TZ <= 8 ? 2 : 1)
     k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap prev_map,
               const __grid_constant__ CUtensorMap a_map, const StencilTables t, const StencilArgs a)
 {

@@ -15,7 +15,8 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_lib", "libsemgb.so")
+# SEMGB_LIBRARY selects another build of the library (same ABI), e.g. one with other tile sizes
+LIB_PATH = os.environ.get("SEMGB_LIBRARY") or os.path.join(_HERE, "_lib", "libsemgb.so")
 
 SEM_OK, SEM_ERR_ARG, SEM_ERR_CUDA, SEM_ERR_OOM, SEM_ERR_TIMEOUT, SEM_ERR_UNSTABLE, SEM_ERR_STATE = range(7)
 KERNEL_AUTO, KERNEL_ELEMENT, KERNEL_STENCIL = 0, 1, 2
