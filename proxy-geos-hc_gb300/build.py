@@ -58,7 +58,8 @@ def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(ROOT, "include", "semgb.h")]
+    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(ROOT, "include", "semgb.h"),
+            os.path.join(ROOT, "include", "semgb.hpp"), os.path.join(HERE, "examples", "sem_proxy.cpp")]
     return any(os.path.getmtime(d) > t for d in deps)
 
 
@@ -83,6 +84,14 @@ def build(force: bool = False, verbose: bool = False, defines: list[str] | None 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    if out is None:  # the C++ example driver over include/semgb.hpp
+        exe = os.path.join(OUT_DIR, "sem_proxy")
+        cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+               os.path.join(HERE, "examples", "sem_proxy.cpp"), "-o", exe, "-L", OUT_DIR, "-lsemgb",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"example build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
