@@ -177,13 +177,15 @@ def test_cpp_driver_matches_oracle(semgb_lib, cuda_device):
 
     from oracle import oracle as O
     exe = os.path.join(os.path.dirname(semgb_lib.LIB_PATH), "sem_proxy")
-    out = subprocess.run([exe, "12", "240", "201"], capture_output=True, text=True, check=True).stdout
+    # 12^3 elements of 200 m: the driver's source point (1001, 1001, 1001) lies inside element (5, 5, 5)
+    out = subprocess.run([exe, "12", "2400", "201"], capture_output=True, text=True, check=True).stdout
     vals = [float(v) for v in re.findall(r"after computeOneStep = (\S+)", out)]
     assert len(vals) == 3  # steps 0, 100, 200
-    # same problem on the oracle: 12^3 order 2, h = 20 m, c = 1500, Ricker 10 Hz, dt = 1 ms
+    # same problem on the oracle: 12^3 order 2, h = 200 m, c = 1500, Ricker 10 Hz, dt = 1 ms
     ex = 12
-    e_src = O.element_from_point(ex, ex, ex, 240.0, 240.0, 240.0, 1001.0, 1001.0, 1001.0)
-    P = O.Problem(ex, ex, ex, 2, 240.0, 240.0, 240.0, 1e-3, 201, np.full(ex ** 3, 1500.0, np.float32),
+    e_src = O.element_from_point(ex, ex, ex, 2400.0, 2400.0, 2400.0, 1001.0, 1001.0, 1001.0)
+    assert e_src == 5 + 5 * ex + 5 * ex * ex
+    P = O.Problem(ex, ex, ex, 2, 2400.0, 2400.0, 2400.0, 1e-3, 201, np.full(ex ** 3, 1500.0, np.float32),
                   np.array([e_src], np.int64), O.source_term(201, 1e-3, 10.0, 1)[None],
                   rec_node=np.array([O.connectivity(ex, ex, ex, 2)[e_src, 0]], np.int64))
     _, _, tr = O.run(P)
