@@ -199,6 +199,38 @@ int sem_solver_synchronize(sem_solver *s);
 int sem_solver_time_kernels(sem_solver *s, int n_steps, float *ms);
 
 /* ------------------------------------------------------------------------------------------
+ * Many shots on one mesh (batched form).  The reference runs one source per process
+ * (SEMdata.hpp:13, SEMproxy.cpp:93-119); a batch advances n_shots independent shots that share
+ * the mesh, the velocity model, the sponge and the receiver set, with the shot index innermost
+ * in memory so that all mesh-side work and data are shared.  Same conventions as sem_solver_*.
+ * ------------------------------------------------------------------------------------------ */
+
+typedef struct sem_batch sem_batch;
+
+int sem_batch_create(sem_mesh *mesh, float dt, int n_shots, sem_batch **out);
+int sem_batch_destroy(sem_batch *b);
+int sem_batch_set_stream(sem_batch *b, void *cuda_stream);
+int sem_batch_set_sponge(sem_batch *b, int thickness, float sigma);
+int sem_batch_set_sponge_profile(sem_batch *b, const float *sx, const float *sy, const float *sz);
+/* One source per shot on local node 0 of elements[shot] (-1: no source for that shot), wavelet
+ * [n_shots][n_samples]; as sem_solver_set_sources per shot. */
+int sem_batch_set_sources(sem_batch *b, const int64_t *elements, const float *wavelet, int n_samples);
+int sem_batch_set_source_points(sem_batch *b, const float *xyz, const float *wavelet, int n_samples);
+/* One receiver set for all shots; traces are [steps][n_rec][n_shots]. */
+int sem_batch_set_receiver_nodes(sem_batch *b, int n_rec, const int64_t *nodes);
+int sem_batch_set_receivers(sem_batch *b, int n_rec, const float *xyz);
+/* Enqueue n_steps for every shot (time loop replayed from a captured CUDA graph). */
+int sem_batch_step(sem_batch *b, int n_steps);
+int sem_batch_synchronize(sem_batch *b);
+int sem_batch_get_traces(sem_batch *b, float *out);
+int sem_batch_get_pressure(sem_batch *b, int shot, int level, float *out);
+/* Time n_steps (CUDA events on the batch's stream); advances the batch. */
+int sem_batch_time_step(sem_batch *b, int n_steps, float *ms_per_step);
+/* Time the candidate launch shapes (shots per lane, x-columns per CTA, planes per CTA) on the
+ * current state, keep the fastest, restore the state; any output pointer may be NULL. */
+int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, int *ychunk);
+
+/* ------------------------------------------------------------------------------------------
  * Allocation-free step.  This entry point has no counterpart in the reference.
  * ------------------------------------------------------------------------------------------ */
 

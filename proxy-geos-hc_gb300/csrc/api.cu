@@ -11,73 +11,19 @@
 #include <string>
 #include <vector>
 
-#include "../../include/semgb.h"
-#include "host_util.h"
-#include "kernels.h"
+#include "abi.h"
 #include "stencil.h"
 
 using namespace semgb;
 
-// ----------------------------------------------------------------------------------------------
-// errors
-// ----------------------------------------------------------------------------------------------
-
 static thread_local std::string g_err;
-
-static int fail(int code, const std::string &msg)
-{
-    g_err = msg;
-    return code;
-}
 
 namespace semgb {
 // Sets the message sem_last_error_string() returns (for entry points defined in other files).
 void set_last_error(const std::string &msg) { g_err = msg; }
 }  // namespace semgb
 
-#define CUDA_TRY(call)                                                                       \
-    do {                                                                                     \
-        cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess)                                                               \
-            return fail(e_ == cudaErrorMemoryAllocation ? SEM_ERR_OOM : SEM_ERR_CUDA,        \
-                        std::string(#call) + ": " + cudaGetErrorString(e_));                 \
-    } while (0)
-
-#define GUARD_BEGIN try {
-#define GUARD_END                                                                            \
-    }                                                                                        \
-    catch (const std::bad_alloc &) { return fail(SEM_ERR_OOM, "host allocation failed"); }  \
-    catch (...) { return fail(SEM_ERR_STATE, "unexpected exception"); }
-
-template <class T>
-static cudaError_t dalloc(T **p, size_t n)
-{
-    *p = nullptr;
-    if (n == 0) return cudaSuccess;
-    return cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T));
-}
-
-template <class T>
-static void dfree(T *&p)
-{
-    if (p) cudaFree(p);
-    p = nullptr;
-}
-
-// ----------------------------------------------------------------------------------------------
-// handles
-// ----------------------------------------------------------------------------------------------
-
-struct sem_mesh {
-    Box box;
-    Gll gll;
-    Geometry geo;
-    int device = 0;
-    float *d_vel = nullptr;     // [n_elem]
-    float *d_slow2 = nullptr;   // [n_nodes] when the node model is active
-    int32_t *d_conn = nullptr;  // [n_elem * npe], built on first use by the element kernel
-    uint64_t model_version = 1;
-};
+static int fail(int code, const std::string &msg) { return sem_fail(code, msg); }
 
 struct sem_solver {
     sem_mesh *mesh = nullptr;

@@ -1,0 +1,495 @@
+// batch_api.cu -- C ABI of the many-shot form (sem_batch_*): shots that share one mesh, model,
+// sponge and receiver set advance together (k_batch.cu); the time loop is replayed from a
+// captured CUDA graph and the launch shape is picked by a timing autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "abi.h"
+#include "batch.h"
+
+using namespace semgb;
+
+struct sem_batch {
+    sem_mesh *mesh = nullptr;
+    float dt = 0;
+    int nshot = 0;
+    int64_t s_pad = 0;
+    int64_t n_int = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    float *d_p[2] = {nullptr, nullptr};  // [n_int][s_pad]
+    int cur = 0;
+    float *d_a = nullptr;
+    uint64_t a_version = 0;
+    double *d_w = nullptr;
+    bool sponge = false;
+    float *d_sx = nullptr, *d_sy = nullptr, *d_sz = nullptr;
+    int nsamples = 0;
+    int64_t *d_src_node = nullptr;
+    float *d_src_coef = nullptr;
+    float *d_wavelet = nullptr;
+    int nrec = 0;
+    int64_t *d_rec_node = nullptr;
+    float *d_traces = nullptr;  // [cap][nrec][nshot]
+    int64_t trace_cap = 0;
+    int *d_ctr = nullptr;
+    int64_t steps_done = 0;
+    BatchTuning tune;
+    bool tuned = false;
+    cudaGraphExec_t graph2[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+void invalidate(sem_batch *b)
+{
+    for (auto &g : b->graph2)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+bool tables_uploaded = false;
+
+cudaError_t ensure_tables()
+{
+    if (tables_uploaded) return cudaSuccess;
+    constexpr int kT = kMaxOrder * (2 * kMaxOrder + 1);
+    std::vector<float> T(kMaxOrder * kT, 0.f), wa(kMaxOrder * kMaxOrder, 0.f);
+    for (int o = 1; o <= kMaxOrder; o++) {
+        Gll g;
+        gll_tables(o, g);
+        stencil_table(g, T.data() + (o - 1) * kT);
+        for (int l = 0; l < o; l++) wa[(o - 1) * kMaxOrder + l] = (float)(l == 0 ? g.w[0] + g.w[o] : g.w[l]);
+    }
+    cudaError_t e = batch_kernel_setup(T.data(), wa.data());
+    if (e == cudaSuccess) tables_uploaded = true;
+    return e;
+}
+
+BatchArgs args_for(const sem_batch *b, int c)
+{
+    const Box &x = b->mesh->box;
+    BatchArgs a{};
+    a.cur = b->d_p[c];
+    a.prev = b->d_p[1 - c];
+    a.a = b->d_a;
+    a.sx = b->d_sx; a.sy = b->d_sy; a.sz = b->d_sz;
+    a.nx = x.nx; a.nxp = x.nxp; a.ny = x.ny; a.nz = x.nz;
+    a.s_pad = b->s_pad;
+    a.ychunk = b->tune.ychunk > 0 ? b->tune.ychunk : (int)x.ny;
+    for (int d = 0; d < 3; d++) a.g[d] = (float)b->mesh->geo.g[d];
+    return a;
+}
+
+cudaError_t enqueue(sem_batch *b, int c)
+{
+    BatchSourceArgs sa{b->d_p[c], b->d_src_node, b->d_src_coef, b->d_wavelet, b->nsamples > 0 ? b->nshot : 0,
+                       b->nsamples, b->s_pad, b->d_ctr};
+    cudaError_t e = launch_batch_source(sa, b->d_ctr, b->stream);
+    if (e != cudaSuccess) return e;
+    e = launch_batch_step(b->mesh->box.order, args_for(b, c), b->sponge, b->tune, b->stream);
+    if (e != cudaSuccess) return e;
+    BatchRecordArgs ra{b->d_p[1 - c], b->d_rec_node, b->nrec, b->nshot, b->s_pad, b->d_traces, b->d_ctr};
+    return launch_batch_record(ra, b->stream);
+}
+
+int prepare(sem_batch *b, int64_t n_new)
+{
+    sem_mesh *m = b->mesh;
+    if (b->a_version != m->model_version) {
+        CUDA_TRY(launch_mass(b->d_a, m->d_slow2 ? nullptr : m->d_vel, m->d_slow2, m->box.ex, m->box.ey, m->box.ez,
+                             m->box.order, m->box.nxp, b->d_w, m->geo.detJ, (double)b->dt * b->dt, b->stream));
+        b->a_version = m->model_version;
+    }
+    if (b->nrec > 0 && b->steps_done + n_new > b->trace_cap) {
+        const int64_t cap = std::max<int64_t>(b->steps_done + n_new, std::max<int64_t>(64, 2 * b->trace_cap));
+        float *nt = nullptr;
+        const size_t per = (size_t)b->nrec * b->nshot;
+        CUDA_TRY(dalloc(&nt, (size_t)cap * per));
+        CUDA_TRY(cudaMemsetAsync(nt, 0, (size_t)cap * per * 4, b->stream));
+        if (b->d_traces && b->steps_done > 0)
+            CUDA_TRY(cudaMemcpyAsync(nt, b->d_traces, (size_t)b->steps_done * per * 4, cudaMemcpyDeviceToDevice, b->stream));
+        CUDA_TRY(cudaStreamSynchronize(b->stream));
+        dfree(b->d_traces);
+        b->d_traces = nt;
+        b->trace_cap = cap;
+        invalidate(b);
+    }
+    return SEM_OK;
+}
+
+// Launch shapes the autotuner tries: shots per lane that divide the padded batch, 4-16 x-columns
+// per CTA, and whole columns or y-chunks long enough to amortise the 2o-plane queue warm-up.
+std::vector<BatchTuning> candidates(const sem_batch *b)
+{
+    std::vector<BatchTuning> v;
+    const int64_t ny = b->mesh->box.ny;
+    for (int spl : {1, 2, 4}) {
+        if (b->s_pad % (32 * spl)) continue;
+        for (int wpc : {4, 8, 16})
+            for (int64_t chunk : {ny, (ny + 1) / 2, (ny + 3) / 4}) {
+                if (chunk < 16 * b->mesh->box.order && chunk != ny) continue;
+                BatchTuning t;
+                t.shots_per_lane = spl;
+                t.warps_per_cta = wpc;
+                t.ychunk = (int)chunk;
+                v.push_back(t);
+            }
+    }
+    return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sem_batch_destroy(sem_batch *b)
+{
+    if (!b) return SEM_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    invalidate(b);
+    for (auto &p : b->d_p) dfree(p);
+    dfree(b->d_a);
+    dfree(b->d_w);
+    dfree(b->d_sx); dfree(b->d_sy); dfree(b->d_sz);
+    dfree(b->d_src_node); dfree(b->d_src_coef); dfree(b->d_wavelet);
+    dfree(b->d_rec_node);
+    dfree(b->d_traces);
+    dfree(b->d_ctr);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return SEM_OK;
+}
+
+int sem_batch_create(sem_mesh *m, float dt, int n_shots, sem_batch **out)
+{
+    GUARD_BEGIN
+    if (!m || !out) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    if (!(dt > 0) || n_shots < 1) return sem_fail(SEM_ERR_ARG, "dt must be positive and n_shots >= 1");
+    sem_batch *b = new sem_batch();
+    b->mesh = m;
+    b->dt = dt;
+    b->nshot = n_shots;
+    b->s_pad = (n_shots + 31) / 32 * 32;
+    b->n_int = m->box.n_int;
+    auto cleanup = [&](int code, const std::string &msg) {
+        sem_batch_destroy(b);
+        return sem_fail(code, msg);
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
+    b->own_stream = true;
+    const size_t n = (size_t)b->n_int * b->s_pad;
+    for (auto &p : b->d_p)
+        if ((e = dalloc(&p, n)) != cudaSuccess || (e = cudaMemset(p, 0, n * 4)) != cudaSuccess)
+            return cleanup(SEM_ERR_OOM, std::string("pressure levels: ") + cudaGetErrorString(e));
+    if ((e = dalloc(&b->d_a, b->n_int)) != cudaSuccess || (e = cudaMemset(b->d_a, 0, b->n_int * 4)) != cudaSuccess)
+        return cleanup(SEM_ERR_OOM, cudaGetErrorString(e));
+    if ((e = dalloc(&b->d_ctr, 2)) != cudaSuccess || (e = cudaMemset(b->d_ctr, 0, 8)) != cudaSuccess)
+        return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
+    if ((e = dalloc(&b->d_w, m->box.order + 1)) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_w, m->gll.w, (m->box.order + 1) * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
+    if ((e = ensure_tables()) != cudaSuccess) return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
+    b->tune.shots_per_lane = b->s_pad % 64 == 0 ? 2 : 1;
+    b->tune.warps_per_cta = 8;
+    b->tune.ychunk = 0;
+    *out = b;
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_batch_set_stream(sem_batch *b, void *stream)
+{
+    if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
+    cudaStreamSynchronize(b->stream);
+    invalidate(b);
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    if (stream) {
+        b->stream = (cudaStream_t)stream;
+        b->own_stream = false;
+    } else {
+        CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        b->own_stream = true;
+    }
+    return SEM_OK;
+}
+
+int sem_batch_set_sponge_profile(sem_batch *b, const float *sx, const float *sy, const float *sz)
+{
+    GUARD_BEGIN
+    if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
+    const Box &x = b->mesh->box;
+    cudaStreamSynchronize(b->stream);
+    invalidate(b);
+    if (!sx || !sy || !sz) { b->sponge = false; return SEM_OK; }
+    if (!b->d_sx) {
+        CUDA_TRY(dalloc(&b->d_sx, x.nx));
+        CUDA_TRY(dalloc(&b->d_sy, x.ny));
+        CUDA_TRY(dalloc(&b->d_sz, x.nz));
+    }
+    CUDA_TRY(cudaMemcpy(b->d_sx, sx, x.nx * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(b->d_sy, sy, x.ny * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(b->d_sz, sz, x.nz * 4, cudaMemcpyHostToDevice));
+    b->sponge = true;
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_batch_set_sponge(sem_batch *b, int thickness, float sigma)
+{
+    GUARD_BEGIN
+    if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
+    if (thickness < 0 || !(sigma >= 0)) return sem_fail(SEM_ERR_ARG, "bad sponge parameters");
+    if (thickness == 0) return sem_batch_set_sponge_profile(b, nullptr, nullptr, nullptr);
+    std::vector<float> x, y, z;
+    box_sponge_profile(b->mesh->box, b->mesh->gll, thickness, sigma, x, y, z);
+    return sem_batch_set_sponge_profile(b, x.data(), y.data(), z.data());
+    GUARD_END
+}
+
+int sem_batch_set_sources(sem_batch *b, const int64_t *elements, const float *wavelet, int n_samples)
+{
+    GUARD_BEGIN
+    if (!b || !elements || (n_samples > 0 && !wavelet) || n_samples < 0) return sem_fail(SEM_ERR_ARG, "bad source arrays");
+    const Box &x = b->mesh->box;
+    std::vector<float> vel(x.n_elem);
+    CUDA_TRY(cudaMemcpy(vel.data(), b->mesh->d_vel, x.n_elem * 4, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> node(b->nshot);
+    std::vector<float> coef(b->nshot);
+    for (int s = 0; s < b->nshot; s++) {
+        if (elements[s] < 0) { node[s] = -1; coef[s] = 0.f; continue; }  // a shot without source
+        if (elements[s] >= x.n_elem) return sem_fail(SEM_ERR_ARG, "source element out of range");
+        node[s] = to_internal(x, box_node(x, elements[s], 0));
+        const float c = vel[elements[s]];
+        coef[s] = b->dt * b->dt * c * c;  // as SEMsolver.cpp:41-42 rounds it
+    }
+    cudaStreamSynchronize(b->stream);
+    invalidate(b);
+    dfree(b->d_src_node); dfree(b->d_src_coef); dfree(b->d_wavelet);
+    CUDA_TRY(dalloc(&b->d_src_node, b->nshot));
+    CUDA_TRY(dalloc(&b->d_src_coef, b->nshot));
+    CUDA_TRY(cudaMemcpy(b->d_src_node, node.data(), b->nshot * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(b->d_src_coef, coef.data(), b->nshot * 4, cudaMemcpyHostToDevice));
+    b->nsamples = n_samples;
+    if (n_samples > 0) {
+        CUDA_TRY(dalloc(&b->d_wavelet, (size_t)b->nshot * n_samples));
+        CUDA_TRY(cudaMemcpy(b->d_wavelet, wavelet, (size_t)b->nshot * n_samples * 4, cudaMemcpyHostToDevice));
+    }
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_batch_set_source_points(sem_batch *b, const float *xyz, const float *wavelet, int n_samples)
+{
+    GUARD_BEGIN
+    if (!b || !xyz) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    std::vector<int64_t> el(b->nshot);
+    for (int s = 0; s < b->nshot; s++) el[s] = box_element_from_point(b->mesh->box, xyz[3 * s], xyz[3 * s + 1], xyz[3 * s + 2]);
+    return sem_batch_set_sources(b, el.data(), wavelet, n_samples);
+    GUARD_END
+}
+
+int sem_batch_set_receiver_nodes(sem_batch *b, int n_rec, const int64_t *nodes)
+{
+    GUARD_BEGIN
+    if (!b || n_rec < 0 || (n_rec > 0 && !nodes)) return sem_fail(SEM_ERR_ARG, "bad receiver array");
+    if (b->steps_done > 0) return sem_fail(SEM_ERR_STATE, "receivers must be set before the first step");
+    std::vector<int64_t> q(n_rec);
+    for (int r = 0; r < n_rec; r++) {
+        if (nodes[r] < 0 || nodes[r] >= b->mesh->box.n_nodes) return sem_fail(SEM_ERR_ARG, "receiver node out of range");
+        q[r] = to_internal(b->mesh->box, nodes[r]);
+    }
+    cudaStreamSynchronize(b->stream);
+    invalidate(b);
+    dfree(b->d_rec_node);
+    dfree(b->d_traces);
+    b->trace_cap = 0;
+    b->nrec = n_rec;
+    if (n_rec > 0) {
+        CUDA_TRY(dalloc(&b->d_rec_node, n_rec));
+        CUDA_TRY(cudaMemcpy(b->d_rec_node, q.data(), n_rec * 8, cudaMemcpyHostToDevice));
+    }
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_batch_set_receivers(sem_batch *b, int n_rec, const float *xyz)
+{
+    GUARD_BEGIN
+    if (!b || (n_rec > 0 && !xyz)) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    std::vector<int64_t> nodes(std::max(n_rec, 0));
+    for (int r = 0; r < n_rec; r++)
+        nodes[r] = box_nearest_node(b->mesh->box, b->mesh->gll, xyz[3 * r], xyz[3 * r + 1], xyz[3 * r + 2]);
+    return sem_batch_set_receiver_nodes(b, n_rec, nodes.data());
+    GUARD_END
+}
+
+int sem_batch_step(sem_batch *b, int n_steps)
+{
+    GUARD_BEGIN
+    if (!b || n_steps < 0) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    if (n_steps == 0) return SEM_OK;
+    int rc = prepare(b, n_steps);
+    if (rc) return rc;
+    int done = 0;
+    while (n_steps - done >= 2) {
+        if (!b->graph2[b->cur]) {
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e1 = enqueue(b, b->cur);
+            cudaError_t e2 = e1 == cudaSuccess ? enqueue(b, 1 - b->cur) : e1;
+            cudaError_t e3 = cudaStreamEndCapture(b->stream, &g);
+            if (e2 != cudaSuccess || e3 != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return sem_fail(SEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e2 != cudaSuccess ? e2 : e3));
+            }
+            cudaError_t e4 = cudaGraphInstantiate(&b->graph2[b->cur], g, 0);
+            cudaGraphDestroy(g);
+            if (e4 != cudaSuccess) return sem_fail(SEM_ERR_CUDA, cudaGetErrorString(e4));
+        }
+        CUDA_TRY(cudaGraphLaunch(b->graph2[b->cur], b->stream));
+        done += 2;
+    }
+    if (done < n_steps) {
+        CUDA_TRY(enqueue(b, b->cur));
+        b->cur ^= 1;
+    }
+    b->steps_done += n_steps;
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_batch_synchronize(sem_batch *b)
+{
+    if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    return SEM_OK;
+}
+
+int sem_batch_get_traces(sem_batch *b, float *out)
+{
+    GUARD_BEGIN
+    if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
+    if (b->nrec == 0 || b->steps_done == 0) return SEM_OK;
+    if (!out) return sem_fail(SEM_ERR_ARG, "NULL output");
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(cudaMemcpy(out, b->d_traces, (size_t)b->steps_done * b->nrec * b->nshot * 4, cudaMemcpyDeviceToHost));
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_batch_get_pressure(sem_batch *b, int shot, int level, float *out)
+{
+    GUARD_BEGIN
+    if (!b || !out || shot < 0 || shot >= b->nshot) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    if (level != SEM_LEVEL_CURRENT && level != SEM_LEVEL_PREVIOUS) return sem_fail(SEM_ERR_ARG, "bad level");
+    const Box &x = b->mesh->box;
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    const int idx = level == SEM_LEVEL_CURRENT ? b->cur : 1 - b->cur;
+    // one shot is a strided column of [n_int][s_pad]: gather it with one 2-D copy, then drop the
+    // row padding
+    std::vector<float> col((size_t)x.n_int);
+    CUDA_TRY(cudaMemcpy2D(col.data(), 4, b->d_p[idx] + shot, (size_t)b->s_pad * 4, 4, (size_t)x.n_int,
+                          cudaMemcpyDeviceToHost));
+    int64_t i = 0;
+    for (int64_t r = 0; r < x.nz * x.ny; r++)
+        for (int64_t c = 0; c < x.nx; c++) out[i++] = col[(size_t)r * x.nxp + c];
+    if (level == SEM_LEVEL_PREVIOUS && b->sponge) {
+        std::vector<float> sx(x.nx), sy(x.ny), sz(x.nz);
+        CUDA_TRY(cudaMemcpy(sx.data(), b->d_sx, x.nx * 4, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(sy.data(), b->d_sy, x.ny * 4, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(sz.data(), b->d_sz, x.nz * 4, cudaMemcpyDeviceToHost));
+        i = 0;
+        for (int64_t iy = 0; iy < x.ny; iy++)
+            for (int64_t iz = 0; iz < x.nz; iz++)
+                for (int64_t ix = 0; ix < x.nx; ix++, i++) out[i] = (sx[ix] * sy[iy] * sz[iz]) * out[i];
+    }
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_batch_time_step(sem_batch *b, int n_steps, float *ms_per_step)
+{
+    GUARD_BEGIN
+    if (!b || !ms_per_step || n_steps < 1) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    int rc = prepare(b, n_steps);
+    if (rc == SEM_OK) {
+        cudaEventRecord(e0, b->stream);
+        rc = sem_batch_step(b, n_steps);
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *ms_per_step = ms / n_steps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+    GUARD_END
+}
+
+int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, int *ychunk)
+{
+    GUARD_BEGIN
+    if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
+    // time every candidate on scratch copies of the current levels; the state is restored after
+    const size_t n = (size_t)b->n_int * b->s_pad;
+    std::vector<float> save0, save1;
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    const int64_t steps0 = b->steps_done;
+    const int cur0 = b->cur;
+    int ctr0[2];
+    CUDA_TRY(cudaMemcpy(ctr0, b->d_ctr, 8, cudaMemcpyDeviceToHost));
+    int rc = prepare(b, 4);
+    if (rc) return rc;
+    float *keep[2] = {nullptr, nullptr};
+    for (int i = 0; i < 2; i++) {
+        CUDA_TRY(dalloc(&keep[i], n));
+        CUDA_TRY(cudaMemcpyAsync(keep[i], b->d_p[i], n * 4, cudaMemcpyDeviceToDevice, b->stream));
+    }
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    BatchTuning pick = b->tune;
+    for (const BatchTuning &t : candidates(b)) {
+        b->tune = t;
+        const int order = b->mesh->box.order;
+        cudaError_t err = launch_batch_step(order, args_for(b, b->cur), b->sponge, t, b->stream);  // warm-up
+        cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < 3 && err == cudaSuccess; r++) err = launch_batch_step(order, args_for(b, b->cur), b->sponge, t, b->stream);
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (err == cudaSuccess && ms < best) { best = ms; pick = t; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (int i = 0; i < 2; i++) {
+        CUDA_TRY(cudaMemcpyAsync(b->d_p[i], keep[i], n * 4, cudaMemcpyDeviceToDevice, b->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    for (auto &k : keep) dfree(k);
+    CUDA_TRY(cudaMemcpy(b->d_ctr, ctr0, 8, cudaMemcpyHostToDevice));
+    b->steps_done = steps0;
+    b->cur = cur0;
+    b->tune = pick;
+    b->tuned = true;
+    invalidate(b);
+    if (shots_per_lane) *shots_per_lane = pick.shots_per_lane;
+    if (warps_per_cta) *warps_per_cta = pick.warps_per_cta;
+    if (ychunk) *ychunk = pick.ychunk;
+    return SEM_OK;
+    GUARD_END
+}
+
+}  // extern "C"

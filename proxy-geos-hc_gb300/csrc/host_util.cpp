@@ -68,6 +68,29 @@ bool gll_tables(int order, Gll &g)
     return true;
 }
 
+void stencil_table(const Gll &g, float *T)
+{
+    const int o = g.order, o1 = o + 1, W = 2 * o + 1;
+    double A[kMaxOrder + 1][kMaxOrder + 1];  // A(i, j) = sum_q w_q phi_i'(xi_q) phi_j'(xi_q)
+    for (int i = 0; i < o1; i++)
+        for (int j = 0; j < o1; j++) {
+            double s = 0;
+            for (int q = 0; q < o1; q++) s += g.w[q] * g.dphi[i * o1 + q] * g.dphi[j * o1 + q];
+            A[i][j] = s;
+        }
+    for (int l = 0; l < o; l++)
+        for (int d = -o; d <= o; d++) {
+            double v = 0;
+            if (l == 0) {
+                if (d >= 0) v += A[0][d];       // element to the right (local 0)
+                if (d <= 0) v += A[o][o + d];   // element to the left (local o)
+            } else if (l + d >= 0 && l + d <= o) {
+                v = A[l][l + d];
+            }
+            T[l * W + d + o] = (float)v;
+        }
+}
+
 float ricker(float time_n, float f0, int order)
 {
     // float/double mix of utils.hpp:11-46, kept so the samples match the reference bit for bit

@@ -20,6 +20,12 @@ struct Gll {
 // decimals, and the Lagrange derivative table at the points.  Returns false for a bad order.
 bool gll_tables(int order, Gll &g);
 
+// Assembled 1-D stiffness coupling of the uniform-box operator: T[l*(2o+1) + d + o] couples a node
+// with local index l (0..o-1) to the node d places further along the same axis (|d| <= o); zero
+// outside the node's element (l > 0) or element pair (l == 0).  From A = D^T diag(w) D of one
+// element, in double, rounded once.
+void stencil_table(const Gll &g, float *T);
+
 // Ricker wavelet in the reference's float arithmetic (utils.hpp:11-46).
 float ricker(float t, float f0, int order);
 

@@ -65,31 +65,6 @@ struct Cfg {
     static constexpr uint32_t AUX_TX = sizeof(float) * 2 * TZ * TX;
 };
 
-// Host: T for one order from the GLL tables (double, rounded once).
-void build_T(const Gll &g, float *T)
-{
-    const int o = g.order, o1 = o + 1, W = 2 * o + 1;
-    // element 1-D stiffness A(i, j) = sum_q w_q phi_i'(xi_q) phi_j'(xi_q)
-    double A[6][6];
-    for (int i = 0; i < o1; i++)
-        for (int j = 0; j < o1; j++) {
-            double s = 0;
-            for (int q = 0; q < o1; q++) s += g.w[q] * g.dphi[i * o1 + q] * g.dphi[j * o1 + q];
-            A[i][j] = s;
-        }
-    for (int l = 0; l < o; l++)
-        for (int d = -o; d <= o; d++) {
-            double v = 0;
-            if (l == 0) {
-                if (d >= 0) v += A[0][d];          // element to the right (local 0)
-                if (d <= 0) v += A[o][o + d];      // element to the left (local o)
-            } else if (l + d >= 0 && l + d <= o) {
-                v = A[l][l + d];
-            }
-            T[l * W + d + o] = (float)v;
-        }
-}
-
 // Offsets d with a non-zero coefficient for local index l: [-o, o] for l == 0 (element face),
 // [-l, o-l] otherwise.
 __host__ __device__ constexpr int dlo(int O, int l) { return l == 0 ? -O : -l; }
@@ -514,7 +489,7 @@ cudaError_t stencil_kernel_setup()
     for (int o = 1; o <= kMaxOrder; o++) {
         Gll g;
         gll_tables(o, g);
-        build_T(g, all.data() + (o - 1) * kTMax);
+        stencil_table(g, all.data() + (o - 1) * kTMax);
         for (int l = 0; l < o; l++) wa[(o - 1) * kMaxOrder + l] = (float)(l == 0 ? g.w[0] + g.w[o] : g.w[l]);
     }
     if ((e = cudaMemcpyToSymbol(c_T, all.data(), all.size() * sizeof(float))) != cudaSuccess) return e;

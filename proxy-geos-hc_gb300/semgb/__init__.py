@@ -72,6 +72,21 @@ _SIGS = {
     "sem_solver_synchronize": [_VP],
     "sem_solver_time_kernels": [_VP, C.c_int, _F32P],
     "sem_element_step_noalloc": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int] + [_VP] * 8,
+    "sem_batch_create": [_VP, C.c_float, C.c_int, C.POINTER(_VP)],
+    "sem_batch_destroy": [_VP],
+    "sem_batch_set_stream": [_VP, _VP],
+    "sem_batch_set_sponge": [_VP, C.c_int, C.c_float],
+    "sem_batch_set_sponge_profile": [_VP, _F32P, _F32P, _F32P],
+    "sem_batch_set_sources": [_VP, _I64P, _F32P, C.c_int],
+    "sem_batch_set_source_points": [_VP, _F32P, _F32P, C.c_int],
+    "sem_batch_set_receiver_nodes": [_VP, C.c_int, _I64P],
+    "sem_batch_set_receivers": [_VP, C.c_int, _F32P],
+    "sem_batch_step": [_VP, C.c_int],
+    "sem_batch_synchronize": [_VP],
+    "sem_batch_get_traces": [_VP, _F32P],
+    "sem_batch_get_pressure": [_VP, C.c_int, C.c_int, _F32P],
+    "sem_batch_time_step": [_VP, C.c_int, _F32P],
+    "sem_batch_autotune": [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
 }
 _RESTYPE = {"sem_last_error_string": C.c_char_p}
 
@@ -315,3 +330,85 @@ def solver_from_workload(wl, kernel: int = KERNEL_AUTO):
     s.set_source_points(wl.src_xyz, wav)
     s.set_receivers(wl.rec_xyz)
     return mesh, s
+
+
+class Batch:
+    """Many shots on one mesh (sem_batch_*): shared mesh, model, sponge and receivers."""
+
+    def __init__(self, mesh: Mesh, dt: float, n_shots: int):
+        h = _VP()
+        _check(lib().sem_batch_create(mesh._h, dt, n_shots, C.byref(h)))
+        self._h = h
+        self.mesh = mesh
+        self.n_shots = n_shots
+        self.nrec = 0
+        self.steps = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sem_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle):
+        _check(lib().sem_batch_set_stream(self._h, stream_handle))
+
+    def set_sponge(self, thickness, sigma):
+        _check(lib().sem_batch_set_sponge(self._h, thickness, sigma))
+
+    def set_sponge_profile(self, sx, sy, sz):
+        a, b, c = _f32(sx), _f32(sy), _f32(sz)
+        _check(lib().sem_batch_set_sponge_profile(self._h, _p(a, _F32P), _p(b, _F32P), _p(c, _F32P)))
+
+    def set_sources(self, elements, wavelet):
+        e = _i64(elements)
+        w = _f32(wavelet).reshape(self.n_shots, -1)
+        _check(lib().sem_batch_set_sources(self._h, _p(e, _I64P), _p(w, _F32P), w.shape[1]))
+
+    def set_source_points(self, xyz, wavelet):
+        x = _f32(xyz).reshape(self.n_shots, 3)
+        w = _f32(wavelet).reshape(self.n_shots, -1)
+        _check(lib().sem_batch_set_source_points(self._h, _p(x, _F32P), _p(w, _F32P), w.shape[1]))
+
+    def set_receiver_nodes(self, nodes):
+        n = _i64(nodes)
+        _check(lib().sem_batch_set_receiver_nodes(self._h, len(n), _p(n, _I64P)))
+        self.nrec = len(n)
+
+    def set_receivers(self, xyz):
+        x = _f32(xyz).reshape(-1, 3)
+        _check(lib().sem_batch_set_receivers(self._h, len(x), _p(x, _F32P)))
+        self.nrec = len(x)
+
+    def step(self, n=1):
+        _check(lib().sem_batch_step(self._h, n))
+        self.steps += n
+
+    def synchronize(self):
+        _check(lib().sem_batch_synchronize(self._h))
+
+    def traces(self):
+        out = np.zeros((self.steps, self.nrec, self.n_shots), np.float32)
+        _check(lib().sem_batch_get_traces(self._h, _p(out, _F32P)))
+        return out
+
+    def pressure(self, shot, level=LEVEL_CURRENT):
+        out = np.empty(self.mesh.n_nodes, np.float32)
+        _check(lib().sem_batch_get_pressure(self._h, shot, level, _p(out, _F32P)))
+        return out
+
+    def time_step(self, n):
+        ms = C.c_float()
+        _check(lib().sem_batch_time_step(self._h, n, C.byref(ms)))
+        self.steps += n
+        return ms.value
+
+    def autotune(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().sem_batch_autotune(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"shots_per_lane": a.value, "warps_per_cta": b.value, "ychunk": c.value}

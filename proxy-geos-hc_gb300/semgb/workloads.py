@@ -174,3 +174,23 @@ def small_random(ex, ey, ez, order, steps, seed, h=10.0, nsrc=1, nrec=16, sponge
     return Workload(f"rand_{ex}x{ey}x{ez}_q{order}_s{seed}", ex, ey, ez, order, h, vel, dt, steps,
                     src.astype(np.float32), f0.astype(np.float32), rec.astype(np.float32),
                     sponge_thickness=sponge, sponge_sigma=0.2)
+
+
+def c3_batched_shots(n: int = 100, n_shots: int = 64, steps: int = 800, seed: int = 3) -> Workload:
+    """Batched shots on one mesh: n^3 (100^3) hex elements of 10 m, GLL order 4, the velocity
+    recipe of :func:`c2_plain_scale` with another seed; n_shots (64) Ricker 8 Hz sources on a
+    seeded jittered 8 x 8 grid spanning the undamped part of the surface, at the depth of the
+    plain workload's source (100 m); the 32 x 32 receiver grid of :func:`c2_plain_scale`;
+    800 steps.  ``src_xyz`` / ``f0`` hold one row per shot."""
+    w = c2_plain_scale(n, steps, seed)
+    rng = np.random.default_rng(seed + 1000)
+    L = n * w.h
+    k = int(round(np.sqrt(n_shots)))
+    a = w.sponge_thickness * w.h
+    g = a + (np.arange(k) + 0.5) / k * (L - 2 * a)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    jit = rng.uniform(-0.25, 0.25, (k * k, 2)) * ((L - 2 * a) / k)
+    src = np.stack([X.ravel() + jit[:, 0], Y.ravel() + jit[:, 1], np.full(k * k, 100.0)], 1)[:n_shots]
+    return Workload(f"c3_batched_{n}c_q4_{n_shots}shots", w.ex, w.ey, w.ez, w.order, w.h, w.vel, w.dt,
+                    steps, src.astype(np.float32), np.full(len(src), 8.0, np.float32), w.rec_xyz,
+                    sponge_thickness=w.sponge_thickness)
