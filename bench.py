@@ -50,6 +50,24 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def reduce_max(x: float, ws: int) -> float:
+    """Max of a per-rank value over all ranks (the value itself on one rank)."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, ws: int, t_local_s: float) -> float:
+    """Whole-job throughput of replicas: the units all ranks processed over the slowest rank's
+    time (every rank runs the same workload; no data moves between ranks)."""
+    return units_per_rank * ws / reduce_max(t_local_s, ws)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -240,11 +258,8 @@ def run_ours(args):
     barrier()
     t_ms = ev0.elapsed_time(ev1)
     s.synchronize()
-    t_all = torch.tensor([t_ms], dtype=torch.float64, device="cuda")
-    if ws > 1:
-        dist.all_reduce(t_all, op=dist.ReduceOp.MAX)
-    t_max = float(t_all.item())
-    value = N * args.steps * ws / (t_max / 1e3) / 1e9
+    t_max = reduce_max(t_ms, ws)
+    value = job_rate(N * args.steps, ws, t_ms / 1e3) / 1e9
 
     # per-kernel device time (CUDA events on the solver's stream, un-captured launches)
     kms = [float(x) for x in s.time_kernels(max(5, min(20, args.steps)))]
@@ -293,10 +308,7 @@ def run_ours(args):
         wav_np[0, :] = src_w[(i + 2) % len(src_w)]
         s.step_host(1, wav_np, tr_np)
     t_e2e = time.perf_counter() - t0
-    e2e_all = torch.tensor([t_e2e], dtype=torch.float64, device="cuda")
-    if ws > 1:
-        dist.all_reduce(e2e_all, op=dist.ReduceOp.MAX)
-    e2e_val = N * e2e_steps * ws / float(e2e_all.item()) / 1e9
+    e2e_val = job_rate(N * e2e_steps, ws, t_e2e) / 1e9
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

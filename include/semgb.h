@@ -231,6 +231,41 @@ int sem_batch_time_step(sem_batch *b, int n_steps, float *ms_per_step);
 int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, int *ychunk);
 
 /* ------------------------------------------------------------------------------------------
+ * Adjoint-state gradient.  The reference has no inversion path; this computes, for one shot,
+ *     L = 1/2 sum_n sum_r (d_r^n - obs_r^n)^2
+ * over the traces d of n_steps plain steps (SEMsolver.cpp:21-125 with the sponge and receivers
+ * of sem_solver_*) and its gradient dL/dm with respect to the per-node squared slowness m
+ * (mass M_i = m_i W_i; the mesh model may be element velocities or node slownesses).  The
+ * forward levels are checkpointed every `checkpoint_every` steps on the device; the backward
+ * sweep recomputes each segment and runs the adjoint steps (the same stencil pass, residuals
+ * injected at the interior receiver nodes).  Source coefficients dt^2 c_e^2 are held fixed.
+ * Device memory: (2 n_segments + checkpoint_every + 1) levels.
+ * ------------------------------------------------------------------------------------------ */
+
+typedef struct sem_adjoint sem_adjoint;
+
+int sem_adjoint_create(sem_mesh *mesh, float dt, int n_steps, int checkpoint_every, sem_adjoint **out);
+int sem_adjoint_destroy(sem_adjoint *a);
+int sem_adjoint_set_sponge(sem_adjoint *a, int thickness, float sigma);
+int sem_adjoint_set_sponge_profile(sem_adjoint *a, const float *sx, const float *sy, const float *sz);
+/* As sem_solver_set_sources / sem_solver_set_source_points / sem_solver_set_receiver*. */
+int sem_adjoint_set_sources(sem_adjoint *a, int n_src, const int64_t *elements, const float *wavelet, int n_samples);
+int sem_adjoint_set_source_points(sem_adjoint *a, int n_src, const float *xyz, const float *wavelet, int n_samples);
+int sem_adjoint_set_receiver_nodes(sem_adjoint *a, int n_rec, const int64_t *nodes);
+int sem_adjoint_set_receivers(sem_adjoint *a, int n_rec, const float *xyz);
+/* Forward run from rest with checkpoints; traces [n_steps][n_rec] (NULL: not copied out). */
+int sem_adjoint_forward(sem_adjoint *a, float *traces);
+/* Backward sweep for the residual d - obs ([n_steps][n_rec]); grad [n_nodes] (reference node
+ * numbering) = dL/dm for L = 1/2 |residual|^2; NULL grad keeps it on the device. */
+int sem_adjoint_backward(sem_adjoint *a, const float *residual, float *grad);
+/* Residual from the last forward run and `observed` ([n_steps][n_rec]); loss and grad as above. */
+int sem_adjoint_gradient(sem_adjoint *a, const float *observed, double *loss, float *grad);
+/* Receivers of the adjoint run (for adjoint tests): after sem_adjoint_backward, traces
+ * [n_steps][n_rec] of the adjoint field, row j holding step n = n_steps-1-j. */
+int sem_adjoint_set_adjoint_receiver_nodes(sem_adjoint *a, int n_rec, const int64_t *nodes);
+int sem_adjoint_get_adjoint_traces(sem_adjoint *a, float *out);
+
+/* ------------------------------------------------------------------------------------------
  * Allocation-free step.  This entry point has no counterpart in the reference.
  * ------------------------------------------------------------------------------------------ */
 

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "abi.h"
+#include "solver.h"
 #include "stencil.h"
 
 using namespace semgb;
@@ -25,50 +26,7 @@ void set_last_error(const std::string &msg) { g_err = msg; }
 
 static int fail(int code, const std::string &msg) { return sem_fail(code, msg); }
 
-struct sem_solver {
-    sem_mesh *mesh = nullptr;
-    float dt = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int kernel = SEM_KERNEL_AUTO;
-    int64_t n_int = 0;               // nodes of the device layout
-    float *d_p[2] = {nullptr, nullptr};
-    int cur = 0;                 // index of the current level
-    float *d_y = nullptr;        // element path accumulator
-    float *d_a = nullptr;        // dt^2 / M
-    uint64_t a_version = 0;
-    float *d_tab = nullptr;      // element coefficient table
-    double *d_w = nullptr;       // GLL weights (double) for the mass kernel
-    StencilTables *stencil = nullptr;
-    // sponge
-    bool sponge = false;
-    float *d_sx = nullptr, *d_sy = nullptr, *d_sz = nullptr;
-    // sources
-    int nsrc = 0, nsamples = 0;
-    int64_t *d_src_node = nullptr;
-    float *d_src_coef = nullptr;
-    float *d_wavelet = nullptr;
-    std::vector<int64_t> src_node;
-    std::vector<float> src_coef;
-    // receivers
-    int nrec = 0;
-    int64_t *d_rec_node = nullptr;  // sorted by node
-    int *d_rec_perm = nullptr;      // sorted position -> caller's receiver index
-    std::vector<int64_t> rec_sorted;
-    uint64_t rec_version = 1;
-    float *d_traces = nullptr;      // [trace_cap][nrec]
-    int64_t trace_cap = 0;
-    int64_t traces_checked = 0;
-    int *d_ctr = nullptr;           // [0] next step, [1] step in flight
-    int *d_status = nullptr;        // non-zero after a bounded device wait gave up
-    int *d_upd_rec_off = nullptr;   // receivers grouped by update-kernel block
-    uint64_t upd_rec_version = 0;
-    int64_t steps_done = 0;
-    // graphs: [parity] two steps starting at level `parity`
-    cudaGraphExec_t graph2[2] = {nullptr, nullptr};
-};
-
-static void invalidate_graphs(sem_solver *s)
+void solver_invalidate_graphs(sem_solver *s)
 {
     for (auto &g : s->graph2)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
@@ -77,6 +35,31 @@ static void invalidate_graphs(sem_solver *s)
 static int resolved_kernel(const sem_solver *s)
 {
     return s->kernel == SEM_KERNEL_AUTO ? SEM_KERNEL_STENCIL : s->kernel;
+}
+
+int solver_set_raw_sources(sem_solver *s, int n_src, const int64_t *nodes, const float *coef, const float *wavelet,
+                           int n_samples)
+{
+    cudaStreamSynchronize(s->stream);
+    solver_invalidate_graphs(s);
+    dfree(s->d_src_node);
+    dfree(s->d_src_coef);
+    dfree(s->d_wavelet);
+    s->nsrc = n_src;
+    s->nsamples = n_samples;
+    s->src_node.assign(nodes, nodes + n_src);
+    s->src_coef.assign(coef, coef + n_src);
+    if (n_src > 0) {
+        CUDA_TRY(dalloc(&s->d_src_node, n_src));
+        CUDA_TRY(dalloc(&s->d_src_coef, n_src));
+        CUDA_TRY(cudaMemcpy(s->d_src_node, nodes, n_src * 8, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(s->d_src_coef, coef, n_src * 4, cudaMemcpyHostToDevice));
+        if (n_samples > 0) {
+            CUDA_TRY(dalloc(&s->d_wavelet, (size_t)n_src * n_samples));
+            CUDA_TRY(cudaMemcpy(s->d_wavelet, wavelet, (size_t)n_src * n_samples * 4, cudaMemcpyHostToDevice));
+        }
+    }
+    return SEM_OK;
 }
 
 extern "C" {
@@ -292,7 +275,7 @@ int sem_solver_destroy(sem_solver *s)
 {
     if (!s) return SEM_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    invalidate_graphs(s);
+    solver_invalidate_graphs(s);
     for (auto &p : s->d_p) dfree(p);
     dfree(s->d_y);
     dfree(s->d_a);
@@ -368,7 +351,7 @@ int sem_solver_set_stream(sem_solver *s, void *stream)
 {
     if (!s) return fail(SEM_ERR_ARG, "NULL solver");
     cudaStreamSynchronize(s->stream);
-    invalidate_graphs(s);
+    solver_invalidate_graphs(s);
     if (s->own_stream) cudaStreamDestroy(s->stream);
     if (stream) {
         s->stream = (cudaStream_t)stream;
@@ -386,7 +369,7 @@ int sem_solver_set_kernel(sem_solver *s, int kernel)
     if (kernel < SEM_KERNEL_AUTO || kernel > SEM_KERNEL_STENCIL) return fail(SEM_ERR_ARG, "unknown kernel");
     if (kernel != s->kernel) {
         cudaStreamSynchronize(s->stream);
-        invalidate_graphs(s);
+        solver_invalidate_graphs(s);
         s->kernel = kernel;
     }
     return SEM_OK;
@@ -398,7 +381,7 @@ int sem_solver_set_sponge_profile(sem_solver *s, const float *sx, const float *s
     if (!s) return fail(SEM_ERR_ARG, "NULL solver");
     const Box &b = s->mesh->box;
     cudaStreamSynchronize(s->stream);
-    invalidate_graphs(s);
+    solver_invalidate_graphs(s);
     if (!sx || !sy || !sz) {
         s->sponge = false;
         return SEM_OK;
@@ -453,26 +436,7 @@ int sem_solver_set_sources(sem_solver *s, int n_src, const int64_t *elements, co
         const float c = vel[elements[k]];
         coef[k] = dt * dt * c * c;              // rounded as SEMsolver.cpp:41-42
     }
-    cudaStreamSynchronize(s->stream);
-    invalidate_graphs(s);
-    dfree(s->d_src_node);
-    dfree(s->d_src_coef);
-    dfree(s->d_wavelet);
-    s->nsrc = n_src;
-    s->nsamples = n_samples;
-    s->src_node = node;
-    s->src_coef = coef;
-    if (n_src > 0) {
-        CUDA_TRY(dalloc(&s->d_src_node, n_src));
-        CUDA_TRY(dalloc(&s->d_src_coef, n_src));
-        CUDA_TRY(cudaMemcpy(s->d_src_node, node.data(), n_src * 8, cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMemcpy(s->d_src_coef, coef.data(), n_src * 4, cudaMemcpyHostToDevice));
-        if (n_samples > 0) {
-            CUDA_TRY(dalloc(&s->d_wavelet, (size_t)n_src * n_samples));
-            CUDA_TRY(cudaMemcpy(s->d_wavelet, wavelet, (size_t)n_src * n_samples * 4, cudaMemcpyHostToDevice));
-        }
-    }
-    return SEM_OK;
+    return solver_set_raw_sources(s, n_src, node.data(), coef.data(), wavelet, n_samples);
     GUARD_END
 }
 
@@ -503,7 +467,7 @@ int sem_solver_set_receiver_nodes(sem_solver *s, int n_rec, const int64_t *nodes
     std::vector<int64_t> sorted(n_rec);  // device-layout indices (same order as reference indices)
     for (int r = 0; r < n_rec; r++) sorted[r] = to_internal(s->mesh->box, nodes[perm[r]]);
     cudaStreamSynchronize(s->stream);
-    invalidate_graphs(s);
+    solver_invalidate_graphs(s);
     dfree(s->d_rec_node);
     dfree(s->d_rec_perm);
     dfree(s->d_traces);
@@ -535,7 +499,9 @@ int sem_solver_set_receivers(sem_solver *s, int n_rec, const float *xyz)
 
 // ---- time loop --------------------------------------------------------------------------------
 
-static int prepare(sem_solver *s, int64_t n_new)
+}  // extern "C"
+
+int solver_prepare(sem_solver *s, int64_t n_new)
 {
     sem_mesh *m = s->mesh;
     const int kern = resolved_kernel(s);
@@ -563,7 +529,7 @@ static int prepare(sem_solver *s, int64_t n_new)
                 CUDA_TRY(cudaMemcpy(s->d_upd_rec_off, off.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
             }
             s->upd_rec_version = s->rec_version;
-            invalidate_graphs(s);
+            solver_invalidate_graphs(s);
         }
     } else {
         if (!s->stencil) {
@@ -574,7 +540,7 @@ static int prepare(sem_solver *s, int64_t n_new)
             return fail(SEM_ERR_CUDA, "tensor-map encoding failed (driver entry point cuTensorMapEncodeTiled)");
         if (s->stencil->rec_version != s->rec_version) {
             CUDA_TRY(stencil_set_receivers(*s->stencil, s->rec_sorted.data(), s->nrec, s->rec_version));
-            invalidate_graphs(s);
+            solver_invalidate_graphs(s);
         }
     }
     if (s->nrec > 0 && s->steps_done + n_new > s->trace_cap) {
@@ -589,14 +555,15 @@ static int prepare(sem_solver *s, int64_t n_new)
         dfree(s->d_traces);
         s->d_traces = nt;
         s->trace_cap = cap;
-        invalidate_graphs(s);
+        solver_invalidate_graphs(s);
     }
     return SEM_OK;
 }
 
 // One step with the current level index c; the new level lands in 1-c.  Optional events time
-// the source, stiffness and update launches.
-static cudaError_t enqueue_step(sem_solver *s, int c, cudaEvent_t *ev = nullptr)
+// the source, stiffness and update launches; `extra` selects an adjoint-support mode of the
+// stencil pass (its side buffers for this step).
+cudaError_t solver_enqueue_step(sem_solver *s, int c, cudaEvent_t *ev, const StepExtra *extra)
 {
     sem_mesh *m = s->mesh;
     const Box &b = m->box;
@@ -607,6 +574,7 @@ static cudaError_t enqueue_step(sem_solver *s, int c, cudaEvent_t *ev = nullptr)
     if ((e = launch_source(sa, s->stream)) != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[1], s->stream);
     if (resolved_kernel(s) == SEM_KERNEL_ELEMENT) {
+        if (extra && extra->mode != STENCIL_PLAIN) return cudaErrorInvalidValue;  // stencil pass only
         ElementArgs ea{};
         ea.conn = m->d_conn;
         ea.p = s->d_p[c];
@@ -647,19 +615,27 @@ static cudaError_t enqueue_step(sem_solver *s, int c, cudaEvent_t *ev = nullptr)
         ta.nrec = s->nrec;
         ta.traces = s->d_traces;
         ta.ctr = s->d_ctr;
-        if ((e = launch_stencil(*s->stencil, ta, c, s->sponge, s->stream)) != cudaSuccess) return e;
+        int mode = STENCIL_PLAIN;
+        if (extra) {
+            mode = extra->mode;
+            ta.kp = extra->kp;
+            ta.grad = extra->grad;
+        }
+        if ((e = launch_stencil(*s->stencil, ta, c, s->sponge, s->stream, mode)) != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[2], s->stream);
     }
     if (ev) cudaEventRecord(ev[3], s->stream);
     return cudaSuccess;
 }
 
+extern "C" {
+
 static int build_graph(sem_solver *s, int c)
 {
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e1 = enqueue_step(s, c);
-    cudaError_t e2 = e1 == cudaSuccess ? enqueue_step(s, 1 - c) : e1;
+    cudaError_t e1 = solver_enqueue_step(s, c);
+    cudaError_t e2 = e1 == cudaSuccess ? solver_enqueue_step(s, 1 - c) : e1;
     cudaError_t e3 = cudaStreamEndCapture(s->stream, &g);
     if (e2 != cudaSuccess || e3 != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -678,7 +654,7 @@ int sem_solver_step(sem_solver *s, int n_steps)
     if (!s) return fail(SEM_ERR_ARG, "NULL solver");
     if (n_steps < 0) return fail(SEM_ERR_ARG, "n_steps must be >= 0");
     if (n_steps == 0) return SEM_OK;
-    int rc = prepare(s, n_steps);
+    int rc = solver_prepare(s, n_steps);
     if (rc) return rc;
     int done = 0;
     while (n_steps - done >= 2) {
@@ -690,7 +666,7 @@ int sem_solver_step(sem_solver *s, int n_steps)
         done += 2;  // two swaps: the current level index is unchanged
     }
     if (done < n_steps) {
-        CUDA_TRY(enqueue_step(s, s->cur));
+        CUDA_TRY(solver_enqueue_step(s, s->cur));
         s->cur ^= 1;
         done++;
     }
@@ -857,13 +833,13 @@ int sem_solver_time_kernels(sem_solver *s, int n_steps, float *ms)
 {
     GUARD_BEGIN
     if (!s || !ms || n_steps < 1) return fail(SEM_ERR_ARG, "bad arguments");
-    int rc = prepare(s, n_steps);
+    int rc = solver_prepare(s, n_steps);
     if (rc) return rc;
     cudaEvent_t ev[4];
     for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
     double acc[3] = {0, 0, 0};
     for (int i = 0; i < n_steps; i++) {
-        cudaError_t e = enqueue_step(s, s->cur, ev);
+        cudaError_t e = solver_enqueue_step(s, s->cur, ev);
         if (e != cudaSuccess) {
             for (auto &x : ev) cudaEventDestroy(x);
             return fail(SEM_ERR_CUDA, cudaGetErrorString(e));

@@ -101,74 +101,144 @@ struct Queue {  // neighbour at offset d along y: register queue
     __device__ __forceinline__ Sv<SPL> operator()(int d) const { return q[d + O]; }
 };
 
+// Neighbours of one node along x or z for the compile-time local index L, loaded up front so
+// that every load of a plane is in flight at once (offsets blo..bhi, 0 excluded).
+template <int O, int L, int SPL>
+struct Nbr {
+    static constexpr int lo = blo(O, L), hi = bhi(O, L);
+    Sv<SPL> v[hi - lo + 1];
+    __device__ __forceinline__ void load(const float *c, int64_t stride)
+    {
+#pragma unroll
+        for (int d = lo; d <= hi; d++)
+            if (d != 0) v[d - lo] = ldv<SPL>(c + d * stride);
+    }
+    __device__ __forceinline__ Sv<SPL> operator()(int d) const { return v[d - lo]; }
+};
+
+struct ColumnCtx {
+    const float *cur_col;  // p^n at (x, 0, z), this lane's first shot
+    float *prv_col;
+    const float *a_col;    // dt^2/M at (x, 0, z)
+    int64_t sx_stride, sz_stride, sy_stride, a_ystride;
+    int yb, ye;
+    float sx, sz;              // sponge factors of the column
+    float gx0, gz0, gy0;       // geometric factors g_d
+};
+
+// One interior (x, z) column: x- and z-local indices LX, LZ are compile-time, so every
+// neighbour offset and coefficient is an immediate; the y-local index cycles at run time.
+template <int O, int SPL, bool SPONGE, int LX, int LZ>
+__device__ __forceinline__ void interior_column(const BatchArgs &a, const ColumnCtx &k)
+{
+    const float wx = cb_wa[O - 1][LX], wz = cb_wa[O - 1][LZ];
+    Sv<SPL> q[2 * O + 1];  // p^n at planes y-O..y+O of this column, this lane's shots
+#pragma unroll
+    for (int j = 0; j < 2 * O; j++) {
+        const int yy = k.yb - O + j;
+        if (yy >= 0 && yy < a.ny) q[j] = ldv<SPL>(k.cur_col + yy * k.sy_stride);
+        else
+#pragma unroll
+            for (int t = 0; t < SPL; t++) q[j].v[t] = 0.f;
+    }
+    int ly = k.yb % O;
+    for (int y = k.yb; y < k.ye; y++) {
+        // every load of this plane first
+        const bool top = y + O < a.ny;
+        const Sv<SPL> qn = ldv<SPL>(k.cur_col + (int64_t)(top ? y + O : y) * k.sy_stride);
+        const float *here = k.cur_col + (int64_t)y * k.sy_stride;
+        Nbr<O, LX, SPL> nx;
+        nx.load(here, k.sx_stride);
+        Nbr<O, LZ, SPL> nz;
+        nz.load(here, k.sz_stride);
+        const Sv<SPL> qv = ldv<SPL>(k.prv_col + (int64_t)y * k.sy_stride);
+        const float am = __ldg(k.a_col + (int64_t)y * k.a_ystride);
+        const float s = SPONGE ? k.sx * __ldg(a.sy + y) * k.sz : 1.f;  // (sx*sy)*sz
+        if (top) q[2 * O] = qn;
+        else
+#pragma unroll
+            for (int t = 0; t < SPL; t++) q[2 * O].v[t] = 0.f;
+        const Sv<SPL> c = q[O];
+        Sv<SPL> ax, az;
+#pragma unroll
+        for (int t = 0; t < SPL; t++) ax.v[t] = az.v[t] = 0.f;
+        axis_term<O, LX, SPL>(c, nx, ax);
+        axis_term<O, LZ, SPL>(c, nz, az);
+        const Sv<SPL> ay = axis<O, SPL>(ly, c, Queue<O, SPL>{q});
+        const float wy = cb_wa[O - 1][ly];
+        const float gx = k.gx0 * (wz * wy), gz = k.gz0 * (wx * wy), gy = k.gy0 * (wx * wz);
+        const bool yin = y > 0 && y < a.ny - 1;
+        Sv<SPL> out;
+#pragma unroll
+        for (int t = 0; t < SPL; t++) {
+            const float qd = SPONGE ? s * qv.v[t] : qv.v[t];
+            const float yv = gx * ax.v[t] + gz * az.v[t] + gy * ay.v[t];
+            const float v = yin ? (2.f * c.v[t] - qd) - am * yv : qd;
+            out.v[t] = SPONGE ? s * v : v;
+        }
+        stv<SPL>(k.prv_col + (int64_t)y * k.sy_stride, out);
+#pragma unroll
+        for (int j = 0; j < 2 * O; j++) q[j] = q[j + 1];
+        ly = ly + 1 == O ? 0 : ly + 1;
+    }
+}
+
+// Columns on the x or z faces: Dirichlet nodes keep the damped previous level.
+template <int SPL, bool SPONGE>
+__device__ __forceinline__ void face_column(const BatchArgs &a, const ColumnCtx &k)
+{
+    for (int y = k.yb; y < k.ye; y++) {
+        const Sv<SPL> qv = ldv<SPL>(k.prv_col + (int64_t)y * k.sy_stride);
+        const float s = SPONGE ? k.sx * __ldg(a.sy + y) * k.sz : 1.f;
+        Sv<SPL> out;
+#pragma unroll
+        for (int t = 0; t < SPL; t++) out.v[t] = SPONGE ? s * (s * qv.v[t]) : qv.v[t];
+        stv<SPL>(k.prv_col + (int64_t)y * k.sy_stride, out);
+    }
+}
+
+template <int O, int SPL, bool SPONGE, int LX = 0, int LZ = 0>
+__device__ __forceinline__ void dispatch_column(int lx, int lz, const BatchArgs &a, const ColumnCtx &k)
+{
+    if (lx == LX && lz == LZ) {
+        interior_column<O, SPL, SPONGE, LX, LZ>(a, k);
+        return;
+    }
+    if constexpr (LZ + 1 < O) dispatch_column<O, SPL, SPONGE, LX, LZ + 1>(lx, lz, a, k);
+    else if constexpr (LX + 1 < O) dispatch_column<O, SPL, SPONGE, LX + 1, 0>(lx, lz, a, k);
+}
+
 template <int O, int SPL, bool SPONGE>
-__global__ void __launch_bounds__(1024) k_batch(const BatchArgs a)
+__global__ void __launch_bounds__(512) k_batch(const BatchArgs a)
 {
     const int warps = blockDim.x >> 5;
     const int lane = threadIdx.x & 31;
     const int64_t col = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);  // x fastest
     if (col >= a.nx * a.nz) return;
     const int64_t z = col / a.nx, x = col - z * a.nx;
+    ColumnCtx k;
     const int64_t S = a.s_pad;
-    const int64_t sx_stride = S, sz_stride = a.nxp * S, sy_stride = a.nxp * a.nz * S;
+    k.sx_stride = S;
+    k.sz_stride = a.nxp * S;
+    k.sy_stride = a.nxp * a.nz * S;
+    k.a_ystride = a.nxp * a.nz;
     const int64_t shot0 = (int64_t)blockIdx.z * 32 * SPL + lane * SPL;  // this lane's first shot
-    const int yb = blockIdx.y * a.ychunk;
-    const int ye = (int)min(a.ny, (int64_t)yb + a.ychunk);
-    const int lx = (int)(x % O), lz = (int)(z % O);
+    k.yb = blockIdx.y * a.ychunk;
+    k.ye = (int)min(a.ny, (int64_t)k.yb + a.ychunk);
+    k.cur_col = a.cur + x * S + z * k.sz_stride + shot0;
+    k.prv_col = a.prev + x * S + z * k.sz_stride + shot0;
+    k.a_col = a.a + x + z * a.nxp;
+    k.sx = SPONGE ? __ldg(a.sx + x) : 1.f;
+    k.sz = SPONGE ? __ldg(a.sz + z) : 1.f;
+    k.gx0 = a.g[0];
+    k.gz0 = a.g[1];
+    k.gy0 = a.g[2];
     const bool xz_in = x > 0 && x < a.nx - 1 && z > 0 && z < a.nz - 1;
-    const float wx = cb_wa[O - 1][lx], wz = cb_wa[O - 1][lz];
-    float sxz = 1.f;
-    if (SPONGE) sxz = __ldg(a.sx + x);
-    const float szv = SPONGE ? __ldg(a.sz + z) : 1.f;
-    const float *cur_col = a.cur + x * sx_stride + z * sz_stride + shot0;
-    float *prv_col = a.prev + x * sx_stride + z * sz_stride + shot0;
-    const int64_t acol = x + z * a.nxp;
-
-    Sv<SPL> q[2 * O + 1];  // p^n at planes y-O..y+O of this column, this lane's shots
-#pragma unroll
-    for (int k = 0; k < 2 * O; k++) {
-        const int yy = yb - O + k;
-        if (yy >= 0 && yy < a.ny) q[k] = ldv<SPL>(cur_col + yy * sy_stride);
-        else
-#pragma unroll
-            for (int j = 0; j < SPL; j++) q[k].v[j] = 0.f;
+    if (!xz_in) {
+        face_column<SPL, SPONGE>(a, k);
+        return;
     }
-    for (int y = yb; y < ye; y++) {
-        if (y + O < a.ny) q[2 * O] = ldv<SPL>(cur_col + (int64_t)(y + O) * sy_stride);
-        else
-#pragma unroll
-            for (int j = 0; j < SPL; j++) q[2 * O].v[j] = 0.f;
-        const Sv<SPL> c = q[O];
-        const float *here = cur_col + (int64_t)y * sy_stride;
-        const Sv<SPL> qv = ldv<SPL>(prv_col + (int64_t)y * sy_stride);
-        const float s = SPONGE ? sxz * __ldg(a.sy + y) * szv : 1.f;  // (sx*sy)*sz
-        Sv<SPL> out;
-        if (xz_in && y > 0 && y < a.ny - 1) {
-            const int ly = y % O;
-            const Sv<SPL> ax = axis<O, SPL>(lx, c, Strided<SPL>{here, sx_stride});
-            const Sv<SPL> az = axis<O, SPL>(lz, c, Strided<SPL>{here, sz_stride});
-            const Sv<SPL> ay = axis<O, SPL>(ly, c, Queue<O, SPL>{q});
-            const float wy = cb_wa[O - 1][ly];
-            const float gx = a.g[0] * (wz * wy), gz = a.g[1] * (wx * wy), gy = a.g[2] * (wx * wz);
-            const float am = __ldg(a.a + acol + (int64_t)y * a.nxp * a.nz);
-#pragma unroll
-            for (int k = 0; k < SPL; k++) {
-                const float qd = SPONGE ? s * qv.v[k] : qv.v[k];
-                const float yv = gx * ax.v[k] + gz * az.v[k] + gy * ay.v[k];
-                const float v = (2.f * c.v[k] - qd) - am * yv;
-                out.v[k] = SPONGE ? s * v : v;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < SPL; k++) {
-                const float qd = SPONGE ? s * qv.v[k] : qv.v[k];
-                out.v[k] = SPONGE ? s * qd : qd;
-            }
-        }
-        stv<SPL>(prv_col + (int64_t)y * sy_stride, out);
-#pragma unroll
-        for (int k = 0; k < 2 * O; k++) q[k] = q[k + 1];
-    }
+    dispatch_column<O, SPL, SPONGE>((int)(x % O), (int)(z % O), a, k);
 }
 
 __global__ void k_batch_source(const BatchSourceArgs a)

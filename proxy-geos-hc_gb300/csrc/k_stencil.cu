@@ -144,7 +144,7 @@ struct YPlanes {
     }
 };
 
-template <int O, bool SPONGE>
+template <int O, bool SPONGE, int MODE>
 __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::TZ <= 8 ? 2 : 1)
     k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap prev_map,
               const __grid_constant__ CUtensorMap a_map, const StencilTables t, const StencilArgs a)
@@ -258,20 +258,37 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::TZ <= 8 ? 2 : 1)
             const float wy = c_wa[O - 1][ly];
             const float syv = SPONGE ? __ldg(a.sy + y) : 1.f;
             const float gx = t.g[0] * (wz * wy), gzy = t.g[1] * wy, gyz = t.g[2] * wz;
-            float out[O];
+            float out[O], kp[O];
+            if (MODE == STENCIL_GRADIENT) load_o<O>(a.kp + (dst_col - a.prev) + (int64_t)y * plane_stride, kp);
 #pragma unroll
             for (int j = 0; j < O; j++) {
                 const float wxj = c_wa[O - 1][j];
                 const float s = SPONGE ? sxv[j] * syv * szv : 1.f;  // (sx*sy)*sz
                 const float qd = SPONGE ? s * q[j] : q[j];
                 float v = qd;
+                if (MODE == STENCIL_RECORD_KP) kp[j] = 0.f;
                 if (xb + j > 0 && xb + j < nx - 1 && zin && yin) {
                     const float yv = gx * ax[j] + (gzy * wxj) * az.v[j] + (gyz * wxj) * ay.v[j];
                     v = (2.f * c[j] - qd) - am[j] * yv;
+                    if (MODE == STENCIL_RECORD_KP) kp[j] = yv;
                 }
                 out[j] = xb + j < nx ? (SPONGE ? s * v : v) : 0.f;
             }
             float *dst = dst_col + (int64_t)y * plane_stride;
+            if (MODE != STENCIL_PLAIN) {
+                // side buffers: same device layout as the levels; padding columns stay untouched
+                const int64_t off = dst - a.prev;
+                if (MODE == STENCIL_GRADIENT) {
+                    float g[O];
+                    load_o<O>(a.grad + off, g);
+#pragma unroll
+                    for (int j = 0; j < O; j++) kp[j] = fmaf(c[j], kp[j], g[j]);
+                }
+                float *side = (MODE == STENCIL_GRADIENT ? a.grad : a.kp) + off;
+#pragma unroll
+                for (int j = 0; j < O; j++)
+                    if (xb + j < nx) side[j] = kp[j];
+            }
             if constexpr (O == 4) {
                 if (xb + 4 <= t.nxp) *reinterpret_cast<float4 *>(dst) = make_float4(out[0], out[1], out[2], out[3]);
             } else if constexpr (O == 2) {
@@ -339,24 +356,47 @@ void tile_dims(int order, int &tx, int &tz, int &hx)
     }
 }
 
+template <int O, bool SPONGE, int MODE>
+void launch_om(const dim3 &grid, const LevelMaps &cm, const LevelMaps &pm, const StencilTables &t,
+               const StencilArgs &a, cudaStream_t s)
+{
+    k_stencil<O, SPONGE, MODE><<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.ring, pm.tile, t.amap, t, a);
+}
+
 template <int O>
-cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, cudaStream_t s)
+cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, int mode, cudaStream_t s)
 {
     const dim3 grid(t.grid[0], t.grid[1], t.grid[2]);
     const LevelMaps &cm = t.lv[ci], &pm = t.lv[1 - ci];
-    if (sponge)
-        k_stencil<O, true><<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.ring, pm.tile, t.amap, t, a);
-    else
-        k_stencil<O, false><<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.ring, pm.tile, t.amap, t, a);
+    switch (mode * 2 + (sponge ? 1 : 0)) {
+    case 0: launch_om<O, false, STENCIL_PLAIN>(grid, cm, pm, t, a, s); break;
+    case 1: launch_om<O, true, STENCIL_PLAIN>(grid, cm, pm, t, a, s); break;
+    case 2: launch_om<O, false, STENCIL_RECORD_KP>(grid, cm, pm, t, a, s); break;
+    case 3: launch_om<O, true, STENCIL_RECORD_KP>(grid, cm, pm, t, a, s); break;
+    case 4: launch_om<O, false, STENCIL_GRADIENT>(grid, cm, pm, t, a, s); break;
+    case 5: launch_om<O, true, STENCIL_GRADIENT>(grid, cm, pm, t, a, s); break;
+    default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
+}
+
+template <int O, bool SPONGE, int MODE>
+cudaError_t setup_om()
+{
+    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)Cfg<O>::SMEM);
 }
 
 template <int O>
 cudaError_t setup_o()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_stencil<O, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<O>::SMEM);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_stencil<O, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<O>::SMEM);
+    cudaError_t e;
+    if ((e = setup_om<O, true, STENCIL_PLAIN>()) != cudaSuccess) return e;
+    if ((e = setup_om<O, false, STENCIL_PLAIN>()) != cudaSuccess) return e;
+    if ((e = setup_om<O, true, STENCIL_RECORD_KP>()) != cudaSuccess) return e;
+    if ((e = setup_om<O, false, STENCIL_RECORD_KP>()) != cudaSuccess) return e;
+    if ((e = setup_om<O, true, STENCIL_GRADIENT>()) != cudaSuccess) return e;
+    return setup_om<O, false, STENCIL_GRADIENT>();
 }
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -503,14 +543,16 @@ cudaError_t stencil_kernel_setup()
     return cudaSuccess;
 }
 
-cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, int cur_index, bool sponge, cudaStream_t s)
+cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, int cur_index, bool sponge, cudaStream_t s,
+                           int mode)
 {
+    if (mode != STENCIL_PLAIN && (!a.kp || (mode == STENCIL_GRADIENT && !a.grad))) return cudaErrorInvalidValue;
     switch (t.order) {
-    case 1: return launch_o<1>(t, a, cur_index, sponge, s);
-    case 2: return launch_o<2>(t, a, cur_index, sponge, s);
-    case 3: return launch_o<3>(t, a, cur_index, sponge, s);
-    case 4: return launch_o<4>(t, a, cur_index, sponge, s);
-    case 5: return launch_o<5>(t, a, cur_index, sponge, s);
+    case 1: return launch_o<1>(t, a, cur_index, sponge, mode, s);
+    case 2: return launch_o<2>(t, a, cur_index, sponge, mode, s);
+    case 3: return launch_o<3>(t, a, cur_index, sponge, mode, s);
+    case 4: return launch_o<4>(t, a, cur_index, sponge, mode, s);
+    case 5: return launch_o<5>(t, a, cur_index, sponge, mode, s);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -134,7 +134,39 @@ __global__ void k_mass(float *a, const float *vel, const float *slow2, int ex, i
     }
 }
 
+// g_i <- g_i / m_i with m_i the node's squared slowness, recovered from the stored
+// a_i = dt^2 / (m_i W_i) and the geometric mass W_i (quadrature weight x detJ x adjacent elements),
+// so it holds for element-velocity and node-slowness models alike.
+__global__ void k_grad_scale(float *g, const float *a, int ex, int ey, int ez, int order, int64_t nxp,
+                             const double *w, double detJ, double dt2)
+{
+    const int64_t nx = (int64_t)ex * order + 1, ny = (int64_t)ey * order + 1,
+                  nz = (int64_t)ez * order + 1, n = nxp * ny * nz;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t iy = q / (nxp * nz), r = q - iy * nxp * nz, iz = r / nxp, ix = r - iz * nxp;
+        if (ix >= nx) {
+            g[q] = 0.f;
+            continue;
+        }
+        const double wq = w[ix % order] * w[iz % order] * w[iy % order];
+        int64_t x0, x1, z0, z1, y0, y1;
+        adj_range(ix, order, ex, x0, x1);
+        adj_range(iz, order, ez, z0, z1);
+        adj_range(iy, order, ey, y0, y1);
+        const double W = wq * detJ * (double)((x1 - x0 + 1) * (z1 - z0 + 1) * (y1 - y0 + 1));
+        g[q] = (float)((double)g[q] * (double)a[q] * W / dt2);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_grad_scale(float *g, const float *a, int ex, int ey, int ez, int order, int64_t nxp,
+                              const double *w_dev, double detJ, double dt2, cudaStream_t s)
+{
+    k_grad_scale<<<152 * 16, 256, 0, s>>>(g, a, ex, ey, ez, order, nxp, w_dev, detJ, dt2);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_update(const UpdateArgs &a, bool sponge, cudaStream_t s)
 {

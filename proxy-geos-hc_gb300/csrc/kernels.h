@@ -72,6 +72,9 @@ cudaError_t launch_update(const UpdateArgs &a, bool sponge, cudaStream_t s);
 cudaError_t launch_source(const SourceArgs &a, cudaStream_t s);
 cudaError_t launch_connectivity(int32_t *conn, int ex, int ey, int ez, int order, int64_t nxp,
                                 cudaStream_t s);
+// Gradient with respect to the nodal mass parameter -> with respect to squared slowness: g /= m.
+cudaError_t launch_grad_scale(float *g, const float *a, int ex, int ey, int ez, int order, int64_t nxp,
+                              const double *w_dev, double detJ, double dt2, cudaStream_t s);
 // a_i = dt^2 / M_i from per-element velocity (vel) or per-node squared slowness (slow2, device
 // layout); zero on padding nodes.
 cudaError_t launch_mass(float *a, const float *vel, const float *slow2, int ex, int ey, int ez,

@@ -56,7 +56,14 @@ struct StencilArgs {
     float *traces;
     const int *ctr;
     int *status;               // set non-zero when a bounded wait gives up
+    // adjoint support (device layout, one value per node; unused by the plain step):
+    //   STENCIL_RECORD_KP: kp <- (K p^n) on interior nodes, 0 elsewhere
+    //   STENCIL_GRADIENT:  grad += p^n * kp (kp recorded by a forward pass)
+    float *kp;
+    float *grad;
 };
+
+enum StencilMode { STENCIL_PLAIN = 0, STENCIL_RECORD_KP = 1, STENCIL_GRADIENT = 2 };
 
 // Tables and tiling for a box (no device buffers yet).  Returns 0 or a cudaError_t.
 int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, StencilTables **out);
@@ -68,6 +75,6 @@ void stencil_tables_free(StencilTables *&t);
 cudaError_t stencil_kernel_setup();
 // cur_index: which of the bound pressure buffers is the current level.
 cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, int cur_index, bool sponge,
-                           cudaStream_t s);
+                           cudaStream_t s, int mode = STENCIL_PLAIN);
 
 }  // namespace semgb

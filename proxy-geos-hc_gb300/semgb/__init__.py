@@ -87,6 +87,19 @@ _SIGS = {
     "sem_batch_get_pressure": [_VP, C.c_int, C.c_int, _F32P],
     "sem_batch_time_step": [_VP, C.c_int, _F32P],
     "sem_batch_autotune": [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "sem_adjoint_create": [_VP, C.c_float, C.c_int, C.c_int, C.POINTER(_VP)],
+    "sem_adjoint_destroy": [_VP],
+    "sem_adjoint_set_sponge": [_VP, C.c_int, C.c_float],
+    "sem_adjoint_set_sponge_profile": [_VP, _F32P, _F32P, _F32P],
+    "sem_adjoint_set_sources": [_VP, C.c_int, _I64P, _F32P, C.c_int],
+    "sem_adjoint_set_source_points": [_VP, C.c_int, _F32P, _F32P, C.c_int],
+    "sem_adjoint_set_receiver_nodes": [_VP, C.c_int, _I64P],
+    "sem_adjoint_set_receivers": [_VP, C.c_int, _F32P],
+    "sem_adjoint_forward": [_VP, _F32P],
+    "sem_adjoint_backward": [_VP, _F32P, _F32P],
+    "sem_adjoint_gradient": [_VP, _F32P, _F64P, _F32P],
+    "sem_adjoint_set_adjoint_receiver_nodes": [_VP, C.c_int, _I64P],
+    "sem_adjoint_get_adjoint_traces": [_VP, _F32P],
 }
 _RESTYPE = {"sem_last_error_string": C.c_char_p}
 
@@ -412,3 +425,86 @@ class Batch:
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         _check(lib().sem_batch_autotune(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return {"shots_per_lane": a.value, "warps_per_cta": b.value, "ychunk": c.value}
+
+
+class Adjoint:
+    """Trace-misfit gradient with respect to per-node squared slowness (sem_adjoint_*): one shot,
+    n_steps plain steps, forward levels checkpointed every `checkpoint_every` steps."""
+
+    def __init__(self, mesh: Mesh, dt: float, n_steps: int, checkpoint_every: int = 50):
+        h = _VP()
+        _check(lib().sem_adjoint_create(mesh._h, dt, n_steps, checkpoint_every, C.byref(h)))
+        self._h = h
+        self.mesh = mesh
+        self.n_steps = n_steps
+        self.nrec = 0
+        self.n_adj_rec = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sem_adjoint_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_sponge(self, thickness, sigma):
+        _check(lib().sem_adjoint_set_sponge(self._h, thickness, sigma))
+
+    def set_sponge_profile(self, sx, sy, sz):
+        a, b, c = _f32(sx), _f32(sy), _f32(sz)
+        _check(lib().sem_adjoint_set_sponge_profile(self._h, _p(a, _F32P), _p(b, _F32P), _p(c, _F32P)))
+
+    def set_sources(self, elements, wavelet):
+        e = _i64(elements)
+        w = _f32(wavelet).reshape(len(e), -1)
+        _check(lib().sem_adjoint_set_sources(self._h, len(e), _p(e, _I64P), _p(w, _F32P), w.shape[1]))
+
+    def set_source_points(self, xyz, wavelet):
+        x = _f32(xyz).reshape(-1, 3)
+        w = _f32(wavelet).reshape(len(x), -1)
+        _check(lib().sem_adjoint_set_source_points(self._h, len(x), _p(x, _F32P), _p(w, _F32P), w.shape[1]))
+
+    def set_receiver_nodes(self, nodes):
+        n = _i64(nodes)
+        _check(lib().sem_adjoint_set_receiver_nodes(self._h, len(n), _p(n, _I64P)))
+        self.nrec = len(n)
+
+    def set_receivers(self, xyz):
+        x = _f32(xyz).reshape(-1, 3)
+        _check(lib().sem_adjoint_set_receivers(self._h, len(x), _p(x, _F32P)))
+        self.nrec = len(x)
+
+    def forward(self):
+        """Forward run from rest; returns the traces [n_steps][n_rec]."""
+        out = np.zeros((self.n_steps, self.nrec), np.float32)
+        _check(lib().sem_adjoint_forward(self._h, _p(out, _F32P)))
+        return out
+
+    def backward(self, residual):
+        """Gradient of 1/2 |residual|^2 with respect to squared slowness, [n_nodes]."""
+        r = _f32(residual).reshape(self.n_steps, self.nrec)
+        g = np.zeros(self.mesh.n_nodes, np.float32)
+        _check(lib().sem_adjoint_backward(self._h, _p(r, _F32P), _p(g, _F32P)))
+        return g
+
+    def gradient(self, observed):
+        """(loss, gradient) for the last forward run against observed traces [n_steps][n_rec]."""
+        o = _f32(observed).reshape(self.n_steps, self.nrec)
+        loss = C.c_double()
+        g = np.zeros(self.mesh.n_nodes, np.float32)
+        _check(lib().sem_adjoint_gradient(self._h, _p(o, _F32P), C.byref(loss), _p(g, _F32P)))
+        return loss.value, g
+
+    def set_adjoint_receiver_nodes(self, nodes):
+        n = _i64(nodes)
+        _check(lib().sem_adjoint_set_adjoint_receiver_nodes(self._h, len(n), _p(n, _I64P)))
+        self.n_adj_rec = len(n)
+
+    def adjoint_traces(self):
+        out = np.zeros((self.n_steps, self.n_adj_rec), np.float32)
+        _check(lib().sem_adjoint_get_adjoint_traces(self._h, _p(out, _F32P)))
+        return out
