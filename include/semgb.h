@@ -231,6 +231,27 @@ int sem_batch_time_step(sem_batch *b, int n_steps, float *ms_per_step);
 int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, int *ychunk);
 
 /* ------------------------------------------------------------------------------------------
+ * Groups of independent problems of uneven size (different meshes, orders, models, dt).  The
+ * reference runs one problem per process (SEMproxy.cpp:41-64); a group advances several
+ * solvers together, replaying one CUDA graph per two steps that holds every member's steps as
+ * a parallel branch, so small members fill the SMs that large ones leave idle.  Members keep
+ * their own state and I/O (sem_solver_get_traces etc.); they use the stencil pass.  A solver
+ * belongs to at most one group at a time; the group must be destroyed before its members.
+ * ------------------------------------------------------------------------------------------ */
+
+typedef struct sem_group sem_group;
+
+int sem_group_create(int n_solvers, sem_solver *const *solvers, sem_group **out);
+int sem_group_destroy(sem_group *g);
+/* Every member advances n_steps (enqueued; ordered after earlier work on the members' streams
+ * and before later calls on them). */
+int sem_group_step(sem_group *g, int n_steps);
+/* Wait for the group; then sem_solver_synchronize on every member (status and finite traces). */
+int sem_group_synchronize(sem_group *g);
+/* Time n_steps of the whole group (CUDA events on the group stream); advances the members. */
+int sem_group_time_step(sem_group *g, int n_steps, float *ms_per_step);
+
+/* ------------------------------------------------------------------------------------------
  * Adjoint-state gradient.  The reference has no inversion path; this computes, for one shot,
  *     L = 1/2 sum_n sum_r (d_r^n - obs_r^n)^2
  * over the traces d of n_steps plain steps (SEMsolver.cpp:21-125 with the sponge and receivers

@@ -28,6 +28,7 @@ static int fail(int code, const std::string &msg) { return sem_fail(code, msg); 
 
 void solver_invalidate_graphs(sem_solver *s)
 {
+    s->graph_gen++;
     for (auto &g : s->graph2)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
 }

@@ -242,9 +242,11 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::TZ <= 8 ? 2 : 1)
 #pragma unroll
             for (int j = 0; j < O; j++) {
                 float acc = 0.f;
+                // constant trip count, so that the loop unrolls together with j and every index
+                // below is a constant (a j-dependent range left it rolled, with the arrays in memory)
 #pragma unroll
-                for (int d = dlo(O, j); d <= dhi(O, j); d++) {
-                    if (d == 0) continue;
+                for (int d = -O; d <= O; d++) {
+                    if (d == 0 || d < dlo(O, j) || d > dhi(O, j)) continue;
                     const int m = j + d;  // offset from the thread's first node, in [-O, O]
                     const float v = m < 0 ? left[m + O] : (m < O ? c[m] : right);
                     acc = fmaf(c_T[O - 1][j * (2 * O + 1) + d + O], v - c[j], acc);

@@ -50,6 +50,7 @@ struct sem_solver {
     int64_t steps_done = 0;
     // graphs: [parity] two steps starting at level `parity`
     cudaGraphExec_t graph2[2] = {nullptr, nullptr};
+    uint64_t graph_gen = 0;  // bumped whenever captured launch parameters may have changed
 };
 
 // Side buffers of one stencil pass (modes of k_stencil.cu: record K p, or accumulate a gradient).

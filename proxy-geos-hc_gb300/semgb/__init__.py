@@ -87,6 +87,11 @@ _SIGS = {
     "sem_batch_get_pressure": [_VP, C.c_int, C.c_int, _F32P],
     "sem_batch_time_step": [_VP, C.c_int, _F32P],
     "sem_batch_autotune": [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "sem_group_create": [C.c_int, C.POINTER(_VP), C.POINTER(_VP)],
+    "sem_group_destroy": [_VP],
+    "sem_group_step": [_VP, C.c_int],
+    "sem_group_synchronize": [_VP],
+    "sem_group_time_step": [_VP, C.c_int, C.POINTER(C.c_float)],
     "sem_adjoint_create": [_VP, C.c_float, C.c_int, C.c_int, C.POINTER(_VP)],
     "sem_adjoint_destroy": [_VP],
     "sem_adjoint_set_sponge": [_VP, C.c_int, C.c_float],
@@ -425,6 +430,40 @@ class Batch:
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         _check(lib().sem_batch_autotune(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return {"shots_per_lane": a.value, "warps_per_cta": b.value, "ychunk": c.value}
+
+
+class Group:
+    """Independent solvers of uneven size advanced together (sem_group_*); one CUDA graph per
+    two steps holds every member's steps as a parallel branch."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)  # keeps the members alive while the group exists
+        arr = (_VP * len(self.solvers))(*[s._h for s in self.solvers])
+        h = _VP()
+        _check(lib().sem_group_create(len(self.solvers), arr, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sem_group_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n=1):
+        _check(lib().sem_group_step(self._h, n))
+
+    def synchronize(self):
+        _check(lib().sem_group_synchronize(self._h))
+
+    def time_step(self, n):
+        ms = C.c_float()
+        _check(lib().sem_group_time_step(self._h, n, C.byref(ms)))
+        return ms.value
 
 
 class Adjoint:

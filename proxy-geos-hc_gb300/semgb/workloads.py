@@ -194,3 +194,88 @@ def c3_batched_shots(n: int = 100, n_shots: int = 64, steps: int = 800, seed: in
     return Workload(f"c3_batched_{n}c_q4_{n_shots}shots", w.ex, w.ey, w.ez, w.order, w.h, w.vel, w.dt,
                     steps, src.astype(np.float32), np.full(len(src), 8.0, np.float32), w.rec_xyz,
                     sponge_thickness=w.sponge_thickness)
+
+
+def c3_uneven_batch(n_problems: int = 32, steps: int = 800, seed: int = 31, lo: int = 40, hi: int = 120):
+    """Uneven batch: n_problems (32) independent problems with element counts drawn per axis from
+    [lo, hi] ([40, 120]) and GLL order from {2, 3, 4}, elements of 10 m, each with the velocity
+    recipe of :func:`c2_plain_scale` (its own seed), a Ricker 8 Hz source at 100 m depth centred in
+    x and y, the 32 x 32 receiver grid two elements below the top face and a 20-element sponge
+    (capped at a quarter of the smallest axis); dt at CFL 0.4 per problem."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_problems):
+        ex, ey, ez = (int(v) for v in rng.integers(lo, hi + 1, 3))
+        order = int(rng.choice([2, 3, 4]))
+        h = 10.0
+        r = np.random.default_rng(seed * 1000 + i)
+        vel = layered_velocity(ex, ey, ez, h, 5, 1500.0, 4500.0, r)
+        dt = cfl_dt(h, order, float(vel.max()))
+        gx = (np.arange(32) + 0.5) / 32 * ex * h
+        gy = (np.arange(32) + 0.5) / 32 * ey * h
+        X, Y = np.meshgrid(gx, gy, indexing="ij")
+        rec = np.stack([X.ravel(), Y.ravel(), np.full(X.size, 2 * h)], 1)
+        out.append(Workload(f"uneven_{i}_{ex}x{ey}x{ez}_q{order}", ex, ey, ez, order, h, vel, dt, steps,
+                            np.array([[ex * h / 2, ey * h / 2, 100.0]], np.float32), np.array([8.0], np.float32),
+                            rec.astype(np.float32), sponge_thickness=min(20, min(ex, ey, ez) // 4)))
+    return out
+
+
+def node_coordinates(ex, ey, ez, order, h):
+    """Node coordinates (x, y, z) in the reference node numbering (node = ix + iz*nx + iy*nx*nz),
+    with GLL points inside each element."""
+    xi = np.array(_gll_points(order))
+    def axis(ne):
+        e = np.arange(ne * order + 1) // order
+        l = np.arange(ne * order + 1) - e * order
+        e = np.minimum(e, ne - 1)
+        l = np.where(np.arange(ne * order + 1) == ne * order, order, l)
+        return e * h + (1.0 + xi[l]) * 0.5 * h
+    x, y, z = axis(ex), axis(ey), axis(ez)
+    Y, Z, X = np.meshgrid(y, z, x, indexing="ij")
+    return X.reshape(-1), Y.reshape(-1), Z.reshape(-1)
+
+
+def _gll_points(order):
+    # Gauss-Lobatto-Legendre points: -1, 1 and the roots of P'_order
+    if order == 1:
+        return [-1.0, 1.0]
+    c = np.zeros(order + 1)
+    c[-1] = 1.0
+    inner = np.sort(np.real(np.polynomial.legendre.legroots(np.polynomial.legendre.legder(c))))
+    return [-1.0, *inner.tolist(), 1.0]
+
+
+def c4_adjoint(n: int = 96, order: int = 3, steps: int = 2000, n_shots: int = 16, n_rec: int = 256,
+               seed: int = 4, h: float = 10.0):
+    """Adjoint gradient: n^3 (96^3) elements of 10 m, GLL order 3; true model = two layers
+    (2000 / 3000 m/s, interface at mid-depth) times (1 + 0.1 g) with g a Gaussian bump of radius 8
+    elements at a seeded position in the lower half of the interior; current model = the layered
+    background smoothed over 4 elements in depth; both per node as squared slowness.  n_shots (16)
+    Ricker 8 Hz sources on a seeded jittered 4 x 4 grid at 60 m depth, n_rec (256) receivers on a
+    16 x 16 grid at 20 m depth, steps (2000), dt at CFL 0.4 of 3300 m/s.  Returns a dict."""
+    rng = np.random.default_rng(seed)
+    L = n * h
+    X, Y, Z = node_coordinates(n, n, n, order, h)
+    zi = L / 2
+    width = 4 * h  # smoothing length of the background's interface
+    c_bg = 2000.0 + 1000.0 * 0.5 * (1.0 + np.tanh((Z - zi) / width))
+    c_layers = np.where(Z < zi, 2000.0, 3000.0)
+    centre = np.array([rng.uniform(0.35, 0.65) * L, rng.uniform(0.35, 0.65) * L, rng.uniform(0.55, 0.7) * L])
+    r2 = ((X - centre[0]) ** 2 + (Y - centre[1]) ** 2 + (Z - centre[2]) ** 2) / (8 * h) ** 2
+    c_true = c_layers * (1.0 + 0.1 * np.exp(-r2))
+    k = int(round(np.sqrt(n_shots)))
+    g = (np.arange(k) + 0.5) / k * L
+    SX, SY = np.meshgrid(g, g, indexing="ij")
+    jit = rng.uniform(-0.2, 0.2, (k * k, 2)) * (L / k)
+    src = np.stack([SX.ravel() + jit[:, 0], SY.ravel() + jit[:, 1], np.full(k * k, 60.0)], 1)[:n_shots]
+    m = int(round(np.sqrt(n_rec)))
+    gr = (np.arange(m) + 0.5) / m * L
+    RX, RY = np.meshgrid(gr, gr, indexing="ij")
+    rec = np.stack([RX.ravel(), RY.ravel(), np.full(m * m, 20.0)], 1)[:n_rec]
+    dt = cfl_dt(h, order, 3300.0)
+    return {"name": f"c4_adjoint_{n}c_q{order}", "ex": n, "ey": n, "ez": n, "order": order, "h": h,
+            "m_true": (1.0 / c_true ** 2).astype(np.float32), "m0": (1.0 / c_bg ** 2).astype(np.float32),
+            "vel_elem": np.full(n * n * n, 2000.0, np.float32), "dt": dt, "steps": steps,
+            "src_xyz": src.astype(np.float32), "f0": 8.0, "rec_xyz": rec.astype(np.float32),
+            "checkpoint_every": 50, "sponge_thickness": 10, "sponge_sigma": 0.06}
