@@ -337,11 +337,165 @@ def run_ours(args):
             "clocks": clk.summary(),
             "kernel_ms": {"source": float(kms[0]), "stiffness": float(kms[1]), "update": float(kms[2])},
         }
+        if not args.no_rows and ws == 1:
+            s.close()
+            mesh.close()
+            torch.cuda.synchronize()
+            line["rows"] = {"batched": measure_batched(), "uneven": measure_uneven(), "adjoint": measure_adjoint()}
         print(json.dumps(line), flush=True)
     s.close()
     mesh.close()
     if ws > 1:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------------------------
+# the other rows of the path: batched shots, uneven groups, adjoint gradient (rank 0, after the
+# headline measurement; each frees its device memory before the next)
+# ---------------------------------------------------------------------------------------------
+
+def _ev_time(stream, fn):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def measure_batched(steps: int = 40, n: int = 100, shots: int = 64):
+    """64 shots on one 100^3 Q4 mesh (sem_batch_*, autotuned launch shape) against the plain step
+    of one shot on the same mesh: shot-node-steps/s of both, inputs larger than L2."""
+    import torch
+    import semgb
+    from semgb import workloads as W
+    wl = W.c3_batched_shots(n, shots, 800)
+    mesh = semgb.Mesh(wl.ex, wl.ey, wl.ez, wl.lx, wl.ly, wl.lz, wl.order)
+    mesh.set_velocity(wl.vel)
+    wav = np.stack([semgb.ricker(wl.nsteps, wl.dt, float(f), 1) for f in wl.f0])
+    N = mesh.n_nodes
+    stream = torch.cuda.Stream()
+    s = semgb.Solver(mesh, wl.dt)
+    s.set_kernel(semgb.KERNEL_STENCIL)
+    s.set_stream(stream.cuda_stream)
+    s.set_sponge(wl.sponge_thickness, wl.sponge_sigma)
+    s.set_source_points(wl.src_xyz[:1], wav[:1])
+    s.set_receivers(wl.rec_xyz)
+    s.step(4)
+    plain_ms = _ev_time(stream, lambda: s.step(steps)) / steps
+    s.close()
+    b = semgb.Batch(mesh, wl.dt, shots)
+    b.set_stream(stream.cuda_stream)
+    b.set_sponge(wl.sponge_thickness, wl.sponge_sigma)
+    b.set_source_points(wl.src_xyz, wav)
+    b.set_receivers(wl.rec_xyz)
+    b.step(4)
+    pick = b.autotune()
+    b.step(2)
+    batch_ms = _ev_time(stream, lambda: b.step(steps)) / steps
+    b.synchronize()
+    b.close()
+    mesh.close()
+    plain = N / (plain_ms / 1e3) / 1e9
+    batch = N * shots / (batch_ms / 1e3) / 1e9
+    return {"workload": wl.name, "nodes": N, "shots": shots, "steps": steps,
+            "plain_Gshot_node_steps_per_s": plain, "plain_ms_per_shot_step": plain_ms,
+            "batched_Gshot_node_steps_per_s": batch, "batched_ms_per_step": batch_ms,
+            "speedup_vs_plain": batch / plain, "tuning": pick,
+            "bytes_per_shot_node": 12.0 + 4.0 / shots,
+            "batched_GBps": batch * (12.0 + 4.0 / shots)}
+
+
+def measure_uneven(steps: int = 20):
+    """32 independent problems (per-axis elements in [40, 120], orders {2, 3, 4}) advanced as one
+    group (one multi-branch CUDA graph per two steps) against the same solvers stepped one after
+    another: node-steps/s over the whole batch."""
+    import torch
+    import semgb
+    from semgb import workloads as W
+    wls = W.c3_uneven_batch(32, 800)
+    stream = torch.cuda.Stream()
+    members = [semgb.solver_from_workload(w, semgb.KERNEL_STENCIL) for w in wls]
+    nodes = sum(m.n_nodes for m, _ in members)
+    for _, s in members:
+        s.set_stream(stream.cuda_stream)
+        s.step(2)
+    seq_ms = _ev_time(stream, lambda: [s.step(steps) for _, s in members])
+    g = semgb.Group([s for _, s in members])
+    g.step(2)
+    g.synchronize()
+    grp_ms = g.time_step(steps) * steps
+    g.synchronize()
+    g.close()
+    for m, s in members:
+        s.close()
+        m.close()
+    return {"workload": "c3_uneven_32", "problems": len(wls), "nodes": nodes, "steps": steps,
+            "orders": sorted({w.order for w in wls}),
+            "group_Gnode_steps_per_s": nodes * steps / (grp_ms / 1e3) / 1e9,
+            "sequential_Gnode_steps_per_s": nodes * steps / (seq_ms / 1e3) / 1e9,
+            "speedup_vs_sequential": seq_ms / grp_ms}
+
+
+def measure_adjoint(shots: int = 2, fd_dirs: int = 2, n: int = 96, steps: int = 2000):
+    """Adjoint gradient on the 96^3 Q3 two-layer model (checkpoint every 50 steps): wall time per
+    shot gradient (forward with checkpoints, recompute, adjoint with the imaging term) and a
+    central-difference check along seeded random directions (FP64 reductions)."""
+    import torch
+    import semgb
+    from semgb import workloads as W
+    c = W.c4_adjoint(n=n, steps=steps)
+    mesh = semgb.Mesh(c["ex"], c["ey"], c["ez"], c["ex"] * c["h"], c["ey"] * c["h"], c["ez"] * c["h"], c["order"])
+    mesh.set_velocity(c["vel_elem"])
+    a = semgb.Adjoint(mesh, c["dt"], steps, c["checkpoint_every"])
+    a.set_sponge(c["sponge_thickness"], c["sponge_sigma"])
+    a.set_receivers(c["rec_xyz"])
+    wav = semgb.ricker(steps, c["dt"], c["f0"], 1)[None]
+    N = mesh.n_nodes
+    obs = []
+    mesh.set_slowness2(c["m_true"])
+    for k in range(shots):
+        a.set_source_points(c["src_xyz"][k:k + 1], wav)
+        obs.append(a.forward())
+    mesh.set_slowness2(c["m0"])
+    grad = np.zeros(N, np.float64)
+    loss = 0.0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(shots):
+        a.set_source_points(c["src_xyz"][k:k + 1], wav)
+        a.forward()
+        l, g = a.gradient(obs[k])
+        loss += l
+        grad += g
+    t_grad = (time.perf_counter() - t0) / shots
+    rng = np.random.default_rng(8)
+    checks = []
+    eps = 1e-3
+    for _ in range(fd_dirs):
+        dm = c["m0"].astype(np.float64) * rng.standard_normal(N)
+        lp = []
+        for sgn in (1, -1):
+            mesh.set_slowness2((c["m0"] + sgn * eps * dm).astype(np.float32))
+            tot = 0.0
+            for k in range(shots):
+                a.set_source_points(c["src_xyz"][k:k + 1], wav)
+                d = a.forward().astype(np.float64)
+                tot += 0.5 * float(np.sum((d - obs[k]) ** 2))
+            lp.append(tot)
+        fd = (lp[0] - lp[1]) / (2 * eps)
+        an = float(np.dot(grad, dm))
+        checks.append({"fd": fd, "adjoint": an, "rel_err": abs(fd - an) / abs(fd)})
+    mesh.set_slowness2(c["m0"])
+    a.close()
+    mesh.close()
+    return {"workload": c["name"], "nodes": N, "steps": steps, "shots": shots,
+            "checkpoint_every": c["checkpoint_every"], "loss": loss,
+            "seconds_per_shot_gradient": t_grad,
+            "Gnode_steps_per_s": 3 * N * steps / t_grad / 1e9,
+            "note": "3 passes per gradient: forward with checkpoints, recompute with K.p recorded, adjoint",
+            "fd_checks": checks}
 
 
 def main():
@@ -357,6 +511,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=16, help="cpu_baseline steps")
     ap.add_argument("--ref-elems", type=int, default=32, help="--impl reference sub-box (elements per axis)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-rows", action="store_true", help="skip the batched / uneven / adjoint rows")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -311,6 +311,25 @@ int sem_element_step_noalloc(int ex, int ey, int ez, float lx, float ly, float l
                              const int32_t *conn, float *p_cur, float *p_prev, const float *coef,
                              const float *sx, const float *sy, const float *sz, void *stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Output formats.  One container for traces and snapshots: 8-byte magic, little-endian uint64
+ * header length, UTF-8 JSON header, zero padding to a 64-byte boundary, little-endian float32
+ * samples.  Traces ("SEMTRC01") are stored trace-major (SEG-Y's order: each receiver's whole
+ * series in turn) with dt, receiver and source coordinates and optional caller JSON; the
+ * in-memory arrays stay [n_steps][n_rec] as sem_solver_get_traces gives them.  Snapshots
+ * ("SEMSNP01") hold one x-z plane of a pressure level, rows of x for increasing z, with the node
+ * coordinates; they replace the ASCII slice of SEMmesh::saveSnapShot (SEMmesh.cpp:624-654).
+ * ------------------------------------------------------------------------------------------ */
+
+int sem_traces_write(const char *path, int n_steps, int n_rec, const float *traces, float dt,
+                     const float *rec_xyz, int n_src, const float *src_xyz, const char *extra_json);
+int sem_traces_read_info(const char *path, int *n_steps, int *n_rec, float *dt);
+int sem_traces_read(const char *path, float *traces);
+/* Plane y = y_index (-1: ny/2 - 1, the reference's plane) of a level of the solver. */
+int sem_solver_write_snapshot(sem_solver *s, int level, int y_index, const char *path);
+int sem_snapshot_read_info(const char *path, int *nx, int *nz, int *y_index);
+int sem_snapshot_read(const char *path, float *plane);
+
 #ifdef __cplusplus
 }
 #endif

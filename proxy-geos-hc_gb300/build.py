@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsemgb.so")
 
 SOURCES = ["api.cu", "adjoint_api.cu", "batch_api.cu", "group_api.cu", "k_element.cu", "k_update.cu", "k_stencil.cu", "k_batch.cu", "noalloc.cu",
-           "host_util.cpp"]
+           "host_util.cpp", "formats.cpp"]
 HEADERS = ["abi.h", "solver.h", "batch.h", "kernels.h", "stencil.h", "host_util.h", "tma.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -9,9 +9,9 @@ namespace semgb {
 
 // Tuning knobs the autotuner picks (sem_batch_autotune).
 struct BatchTuning {
-    int shots_per_lane = 2;  // 1, 2 or 4: shots per lane of a warp (a warp covers 32x that)
-    int warps_per_cta = 8;   // x-columns per CTA
-    int ychunk = 0;          // planes per CTA along y (0: whole column)
+    int shots_per_lane = 1;  // one shot per lane: a warp covers 32 shots
+    int warps_per_cta = 4;   // element spans (neighbouring z-rows) per CTA: 2 or 4
+    int ychunk = 0;          // planes per CTA along y, rounded up to whole elements (0: all)
 };
 
 struct BatchArgs {

@@ -121,24 +121,23 @@ int prepare(sem_batch *b, int64_t n_new)
     return SEM_OK;
 }
 
-// Launch shapes the autotuner tries: shots per lane that divide the padded batch, 4-16 x-columns
-// per CTA, and whole columns or y-chunks long enough to amortise the 2o-plane queue warm-up.
+// Launch shapes the autotuner tries: 2 or 4 element spans per CTA, and whole columns or
+// y-chunks of about a quarter or an eighth of the planes (whole elements; the carried partial
+// sum costs one extra element of loads per chunk).
 std::vector<BatchTuning> candidates(const sem_batch *b)
 {
     std::vector<BatchTuning> v;
-    const int64_t ny = b->mesh->box.ny;
-    for (int spl : {1, 2, 4}) {
-        if (b->s_pad % (32 * spl)) continue;
-        for (int wpc : {4, 8, 16})
-            for (int64_t chunk : {ny, (ny + 1) / 2, (ny + 3) / 4}) {
-                if (chunk < 16 * b->mesh->box.order && chunk != ny) continue;
-                BatchTuning t;
-                t.shots_per_lane = spl;
-                t.warps_per_cta = wpc;
-                t.ychunk = (int)chunk;
-                v.push_back(t);
-            }
-    }
+    const int64_t ny = b->mesh->box.ny, o = b->mesh->box.order;
+    for (int wpc : {2, 4})
+        for (int64_t div : {1, 4, 8}) {
+            const int64_t chunk = ((ny + div - 1) / div + o - 1) / o * o;
+            if (div > 1 && chunk < 8 * o) continue;
+            BatchTuning t;
+            t.shots_per_lane = 1;
+            t.warps_per_cta = wpc;
+            t.ychunk = (int)(div == 1 ? ny : chunk);
+            v.push_back(t);
+        }
     return v;
 }
 
@@ -195,9 +194,9 @@ int sem_batch_create(sem_mesh *m, float dt, int n_shots, sem_batch **out)
         (e = cudaMemcpy(b->d_w, m->gll.w, (m->box.order + 1) * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
         return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     if ((e = ensure_tables()) != cudaSuccess) return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
-    b->tune.shots_per_lane = b->s_pad % 64 == 0 ? 2 : 1;
-    b->tune.warps_per_cta = 8;
-    b->tune.ychunk = 0;
+    b->tune.shots_per_lane = 1;
+    b->tune.warps_per_cta = 4;
+    b->tune.ychunk = (int)std::max<int64_t>(8 * m->box.order, (m->box.ny / 8 + m->box.order - 1) / m->box.order * m->box.order);
     *out = b;
     return SEM_OK;
     GUARD_END

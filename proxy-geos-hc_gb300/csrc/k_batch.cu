@@ -1,19 +1,20 @@
 // k_batch.cu -- many shots on one mesh: the SEM step with the shot index innermost.
 //
 // A batch advances S shots (independent sources, same mesh, model, sponge and receivers).  The
-// levels are stored P[node][S] (device layout of the node, S padded to a multiple of 32), so for
-// one node the S shot values are contiguous.  Compared with S separate runs of the plain step:
-//  - the mesh-side data (dt^2/M, sponge factors, node indices, GLL coefficients) is read or
-//    computed once per node for all shots: bytes per shot-node-step fall from 16 to
-//    12 + 4/S (read p^n, p^{n-1}, write p^{n+1}, plus the shared dt^2/M);
-//  - a warp owns one (x, z) node column for 32 * SPL shots (SPL shots per lane) and marches
-//    along y, so every spatial quantity -- node index, local GLL indices, coefficients, mass,
-//    sponge factor -- is warp-uniform and paid once per 32 * SPL shot-nodes, and every load or
-//    store is one contiguous 128 * SPL-byte vector;
-//  - the y-neighbours come from a per-lane register queue of 2o+1 planes (p^n is read from HBM
-//    once per node), the x- and z-neighbours from L1/L2 (the warps of a CTA hold consecutive
-//    x-columns and all resident warps march through the same few planes).
-// The operator is the assembled tensor-product form of stencil.h.
+// levels are stored P[node][S] (device layout of the node, S padded to a multiple of 32), so the
+// S values of one node are contiguous.  Against S runs of the plain step:
+//  - the mesh-side data (dt^2/M, sponge factors, coefficients) is read once per node for all
+//    shots: 12 + 4/S bytes per shot-node-step instead of 16;
+//  - a warp owns one element's x-span (o nodes) in one z-row for 32 shots (one per lane), so every
+//    spatial quantity -- node index, local indices, coefficients, mass, sponge factor -- is
+//    warp-uniform, and every load or store is one contiguous 128-byte line;
+//  - the x-coupling inside the element comes from registers (only the o nodes of the element to
+//    the left and one node to the right are loaded); the z-neighbours come through L1/L2;
+//  - the warp marches along y element by element: o+1 planes of its span in registers and, for
+//    the face plane of the next element, the partial y-sum of the element below, so the y-local
+//    index is a compile-time constant.
+// Per shot the arithmetic is the plain stencil pass's (k_stencil.cu) in the same order: the
+// assembled tensor-product operator of stencil.h, difference form, same sponge product.
 #include <cuda_runtime.h>
 
 #include "batch.h"
@@ -23,222 +24,224 @@ namespace semgb {
 namespace {
 
 constexpr int kTBMax = kMaxOrder * (2 * kMaxOrder + 1);
-__constant__ float cb_T[kMaxOrder][kTBMax];    // same table as the plain stencil
+__constant__ float cb_T[kMaxOrder][kTBMax];
 __constant__ float cb_wa[kMaxOrder][kMaxOrder];
 
 __host__ __device__ constexpr int blo(int O, int l) { return l == 0 ? -O : -l; }
 __host__ __device__ constexpr int bhi(int O, int l) { return l == 0 ? O : O - l; }
 
-template <int SPL>
-struct Sv {
-    float v[SPL];
-};
+template <int O>
+__device__ __forceinline__ float Tc(int l, int d) { return cb_T[O - 1][l * (2 * O + 1) + d + O]; }
 
-template <int SPL>
-__device__ __forceinline__ Sv<SPL> ldv(const float *p)
-{
-    Sv<SPL> r;
-    if constexpr (SPL == 2) {
-        const float2 t = *reinterpret_cast<const float2 *>(p);
-        r.v[0] = t.x; r.v[1] = t.y;
-    } else if constexpr (SPL == 4) {
-        const float4 t = *reinterpret_cast<const float4 *>(p);
-        r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
-    } else {
-        r.v[0] = *p;
-    }
-    return r;
-}
-
-template <int SPL>
-__device__ __forceinline__ void stv(float *p, const Sv<SPL> &a)
-{
-    if constexpr (SPL == 2) *reinterpret_cast<float2 *>(p) = make_float2(a.v[0], a.v[1]);
-    else if constexpr (SPL == 4) *reinterpret_cast<float4 *>(p) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
-    else *p = a.v[0];
-}
-
-// acc += sum_d T[L][d] (nbr(d) - c) for the compile-time local index L (neighbours through `at`).
-template <int O, int L, int SPL, class At>
-__device__ __forceinline__ void axis_term(const Sv<SPL> &c, const At &at, Sv<SPL> &acc)
+// z-term of the O nodes of a row for compile-time z-local index LZ: rows z+d read from memory
+template <int O, int LZ>
+__device__ __forceinline__ void zterm(const float (&c)[O], const float *here, int64_t zs, int64_t S, float (&az)[O])
 {
 #pragma unroll
-    for (int d = blo(O, L); d <= bhi(O, L); d++) {
+    for (int j = 0; j < O; j++) az[j] = 0.f;
+#pragma unroll
+    for (int d = blo(O, LZ); d <= bhi(O, LZ); d++) {
         if (d == 0) continue;
-        const Sv<SPL> v = at(d);
-        const float t = cb_T[O - 1][L * (2 * O + 1) + d + O];
+        const float *row = here + d * zs;
+        const float t = Tc<O>(LZ, d);
 #pragma unroll
-        for (int k = 0; k < SPL; k++) acc.v[k] = fmaf(t, v.v[k] - c.v[k], acc.v[k]);
+        for (int j = 0; j < O; j++) az[j] = fmaf(t, __ldg(row + j * S) - c[j], az[j]);
     }
 }
 
-template <int O, int SPL, class At>
-__device__ __forceinline__ Sv<SPL> axis(int l, const Sv<SPL> &c, const At &at)
+template <int O>
+__device__ __forceinline__ void zterm_rt(int lz, const float (&c)[O], const float *here, int64_t zs, int64_t S,
+                                         float (&az)[O])
 {
-    Sv<SPL> acc;
-#pragma unroll
-    for (int k = 0; k < SPL; k++) acc.v[k] = 0.f;
-    switch (l) {  // warp-uniform
-    case 0: axis_term<O, 0, SPL>(c, at, acc); break;
-    case 1: if constexpr (O > 1) axis_term<O, 1, SPL>(c, at, acc); break;
-    case 2: if constexpr (O > 2) axis_term<O, 2, SPL>(c, at, acc); break;
-    case 3: if constexpr (O > 3) axis_term<O, 3, SPL>(c, at, acc); break;
-    default: if constexpr (O > 4) axis_term<O, 4, SPL>(c, at, acc); break;
+    switch (lz) {
+    case 0: zterm<O, 0>(c, here, zs, S, az); break;
+    case 1: if constexpr (O > 1) zterm<O, 1>(c, here, zs, S, az); break;
+    case 2: if constexpr (O > 2) zterm<O, 2>(c, here, zs, S, az); break;
+    case 3: if constexpr (O > 3) zterm<O, 3>(c, here, zs, S, az); break;
+    default: if constexpr (O > 4) zterm<O, 4>(c, here, zs, S, az); break;
     }
-    return acc;
 }
-
-template <int SPL>
-struct Strided {  // neighbour at offset d: base + d * stride (floats)
-    const float *base;
-    int64_t stride;
-    __device__ __forceinline__ Sv<SPL> operator()(int d) const { return ldv<SPL>(base + d * stride); }
-};
-
-template <int O, int SPL>
-struct Queue {  // neighbour at offset d along y: register queue
-    const Sv<SPL> *q;
-    __device__ __forceinline__ Sv<SPL> operator()(int d) const { return q[d + O]; }
-};
-
-// Neighbours of one node along x or z for the compile-time local index L, loaded up front so
-// that every load of a plane is in flight at once (offsets blo..bhi, 0 excluded).
-template <int O, int L, int SPL>
-struct Nbr {
-    static constexpr int lo = blo(O, L), hi = bhi(O, L);
-    Sv<SPL> v[hi - lo + 1];
-    __device__ __forceinline__ void load(const float *c, int64_t stride)
-    {
-#pragma unroll
-        for (int d = lo; d <= hi; d++)
-            if (d != 0) v[d - lo] = ldv<SPL>(c + d * stride);
-    }
-    __device__ __forceinline__ Sv<SPL> operator()(int d) const { return v[d - lo]; }
-};
 
 struct ColumnCtx {
-    const float *cur_col;  // p^n at (x, 0, z), this lane's first shot
-    float *prv_col;
-    const float *a_col;    // dt^2/M at (x, 0, z)
-    int64_t sx_stride, sz_stride, sy_stride, a_ystride;
-    int yb, ye;
-    float sx, sz;              // sponge factors of the column
-    float gx0, gz0, gy0;       // geometric factors g_d
+    const float *cur0;
+    float *prv0;
+    const float *a0;
+    int64_t S, zs, ys, ays;
+    int ny, ye, exi, lz;
+    bool last;
+    float szv, wz, g0, g1, g2;
 };
 
-// One interior (x, z) column: x- and z-local indices LX, LZ are compile-time, so every
-// neighbour offset and coefficient is an immediate; the y-local index cycles at run time.
-template <int O, int SPL, bool SPONGE, int LX, int LZ>
-__device__ __forceinline__ void interior_column(const BatchArgs &a, const ColumnCtx &k)
+template <int O, bool SPONGE, int K>
+__device__ __forceinline__ void plane_step(const BatchArgs &a, const ColumnCtx &k, int y0, const float (&sxv)[O + 1],
+                                       const float (&P)[O + 1][O], const float (&pend)[O])
 {
-    const float wx = cb_wa[O - 1][LX], wz = cb_wa[O - 1][LZ];
-    Sv<SPL> q[2 * O + 1];  // p^n at planes y-O..y+O of this column, this lane's shots
+    const int y = y0 + K;
+    if (y >= k.ye) return;
+    const float syv = SPONGE ? __ldg(a.sy + y) : 1.f;
+    const float *here = k.cur0 + (int64_t)y * k.ys;
+    float *dst = k.prv0 + (int64_t)y * k.ys;
+    float q[O], am[O];
 #pragma unroll
-    for (int j = 0; j < 2 * O; j++) {
-        const int yy = k.yb - O + j;
-        if (yy >= 0 && yy < a.ny) q[j] = ldv<SPL>(k.cur_col + yy * k.sy_stride);
-        else
-#pragma unroll
-            for (int t = 0; t < SPL; t++) q[j].v[t] = 0.f;
+    for (int j = 0; j < O; j++) {
+        q[j] = dst[j * k.S];
+        am[j] = __ldg(k.a0 + (int64_t)y * k.ays + j);
     }
-    int ly = k.yb % O;
-    for (int y = k.yb; y < k.ye; y++) {
-        // every load of this plane first
-        const bool top = y + O < a.ny;
-        const Sv<SPL> qn = ldv<SPL>(k.cur_col + (int64_t)(top ? y + O : y) * k.sy_stride);
-        const float *here = k.cur_col + (int64_t)y * k.sy_stride;
-        Nbr<O, LX, SPL> nx;
-        nx.load(here, k.sx_stride);
-        Nbr<O, LZ, SPL> nz;
-        nz.load(here, k.sz_stride);
-        const Sv<SPL> qv = ldv<SPL>(k.prv_col + (int64_t)y * k.sy_stride);
-        const float am = __ldg(k.a_col + (int64_t)y * k.a_ystride);
-        const float s = SPONGE ? k.sx * __ldg(a.sy + y) * k.sz : 1.f;  // (sx*sy)*sz
-        if (top) q[2 * O] = qn;
-        else
+    float qR = 0.f;
+    if (k.last) qR = dst[O * k.S];
+    const bool yin = y > 0 && y < k.ny - 1;
+    float out[O];
+    if (yin) {
+        float L[O];
+        if (k.exi > 0) {
 #pragma unroll
-            for (int t = 0; t < SPL; t++) q[2 * O].v[t] = 0.f;
-        const Sv<SPL> c = q[O];
-        Sv<SPL> ax, az;
+            for (int j = 0; j < O; j++) L[j] = __ldg(here + (j - O) * k.S);
+        } else {
 #pragma unroll
-        for (int t = 0; t < SPL; t++) ax.v[t] = az.v[t] = 0.f;
-        axis_term<O, LX, SPL>(c, nx, ax);
-        axis_term<O, LZ, SPL>(c, nz, az);
-        const Sv<SPL> ay = axis<O, SPL>(ly, c, Queue<O, SPL>{q});
-        const float wy = cb_wa[O - 1][ly];
-        const float gx = k.gx0 * (wz * wy), gz = k.gz0 * (wx * wy), gy = k.gy0 * (wx * wz);
-        const bool yin = y > 0 && y < a.ny - 1;
-        Sv<SPL> out;
-#pragma unroll
-        for (int t = 0; t < SPL; t++) {
-            const float qd = SPONGE ? s * qv.v[t] : qv.v[t];
-            const float yv = gx * ax.v[t] + gz * az.v[t] + gy * ay.v[t];
-            const float v = yin ? (2.f * c.v[t] - qd) - am * yv : qd;
-            out.v[t] = SPONGE ? s * v : v;
+            for (int j = 0; j < O; j++) L[j] = 0.f;
         }
-        stv<SPL>(k.prv_col + (int64_t)y * k.sy_stride, out);
+        const float R = __ldg(here + O * k.S);
+        float az[O];
+        zterm_rt<O>(k.lz, P[K], here, k.zs, k.S, az);
+        const float wy = cb_wa[O - 1][K];
+        const float gxz = k.g0 * (k.wz * wy), gz0 = k.g1 * wy, gy0 = k.g2 * k.wz;
 #pragma unroll
-        for (int j = 0; j < 2 * O; j++) q[j] = q[j + 1];
-        ly = ly + 1 == O ? 0 : ly + 1;
-    }
-}
-
-// Columns on the x or z faces: Dirichlet nodes keep the damped previous level.
-template <int SPL, bool SPONGE>
-__device__ __forceinline__ void face_column(const BatchArgs &a, const ColumnCtx &k)
-{
-    for (int y = k.yb; y < k.ye; y++) {
-        const Sv<SPL> qv = ldv<SPL>(k.prv_col + (int64_t)y * k.sy_stride);
-        const float s = SPONGE ? k.sx * __ldg(a.sy + y) * k.sz : 1.f;
-        Sv<SPL> out;
+        for (int j = 0; j < O; j++) {
+            const float c = P[K][j];
+            float ax = 0.f;
 #pragma unroll
-        for (int t = 0; t < SPL; t++) out.v[t] = SPONGE ? s * (s * qv.v[t]) : qv.v[t];
-        stv<SPL>(k.prv_col + (int64_t)y * k.sy_stride, out);
+            for (int d = -O; d <= O; d++) {  // constant trip count: fully unrolled with j
+                if (d == 0 || d < blo(O, j) || d > bhi(O, j)) continue;
+                const int m = j + d;
+                float v;  // selected by value: an lvalue conditional would put the arrays in memory
+                if (m < 0) v = L[m + O];
+                else if (m < O) v = P[K][m];
+                else v = R;
+                ax = fmaf(Tc<O>(j, d), v - c, ax);
+            }
+            float ay = K == 0 ? pend[j] : 0.f;
+#pragma unroll
+            for (int d = blo(O, K); d <= bhi(O, K); d++) {
+                if (d == 0 || (K == 0 && d < 0)) continue;
+                ay = fmaf(Tc<O>(K, d), P[K + d][j] - c, ay);
+            }
+            const float s = SPONGE ? sxv[j] * syv * k.szv : 1.f;
+            const float qd = SPONGE ? s * q[j] : q[j];
+            const float wxj = cb_wa[O - 1][j];
+            const float yv = gxz * ax + (gz0 * wxj) * az[j] + (gy0 * wxj) * ay;
+            float v = (2.f * c - qd) - am[j] * yv;
+            if (j == 0 && k.exi == 0) v = qd;  // x = 0 face
+            out[j] = SPONGE ? s * v : v;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < O; j++) {
+            const float s = SPONGE ? sxv[j] * syv * k.szv : 1.f;
+            out[j] = SPONGE ? s * (s * q[j]) : q[j];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < O; j++) dst[j * k.S] = out[j];
+    if (k.last) {
+        const float s = SPONGE ? sxv[O] * syv * k.szv : 1.f;
+        dst[O * k.S] = SPONGE ? s * (s * qR) : qR;
     }
 }
 
-template <int O, int SPL, bool SPONGE, int LX = 0, int LZ = 0>
-__device__ __forceinline__ void dispatch_column(int lx, int lz, const BatchArgs &a, const ColumnCtx &k)
+template <int O, bool SPONGE, int K = 0>
+__device__ __forceinline__ void element_planes(const BatchArgs &a, const ColumnCtx &k, int y0, const float (&sxv)[O + 1],
+                                        const float (&P)[O + 1][O], const float (&pend)[O])
 {
-    if (lx == LX && lz == LZ) {
-        interior_column<O, SPL, SPONGE, LX, LZ>(a, k);
-        return;
-    }
-    if constexpr (LZ + 1 < O) dispatch_column<O, SPL, SPONGE, LX, LZ + 1>(lx, lz, a, k);
-    else if constexpr (LX + 1 < O) dispatch_column<O, SPL, SPONGE, LX + 1, 0>(lx, lz, a, k);
+    plane_step<O, SPONGE, K>(a, k, y0, sxv, P, pend);
+    if constexpr (K + 1 < O) element_planes<O, SPONGE, K + 1>(a, k, y0, sxv, P, pend);
 }
 
-template <int O, int SPL, bool SPONGE>
-__global__ void __launch_bounds__(512) k_batch(const BatchArgs a)
+template <int O, bool SPONGE>
+__global__ void __launch_bounds__(128, 4) k_batch(const BatchArgs a, int ex)
 {
     const int warps = blockDim.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int64_t col = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);  // x fastest
-    if (col >= a.nx * a.nz) return;
-    const int64_t z = col / a.nx, x = col - z * a.nx;
+    const int64_t wid = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
+    const int64_t nz = a.nz;
+    if (wid >= (int64_t)ex * nz) return;
+    const int z = (int)(wid % nz), exi = (int)(wid / nz);  // z fastest: neighbouring rows in one CTA
+    const int x0 = exi * O;
     ColumnCtx k;
-    const int64_t S = a.s_pad;
-    k.sx_stride = S;
-    k.sz_stride = a.nxp * S;
-    k.sy_stride = a.nxp * a.nz * S;
-    k.a_ystride = a.nxp * a.nz;
-    const int64_t shot0 = (int64_t)blockIdx.z * 32 * SPL + lane * SPL;  // this lane's first shot
-    k.yb = blockIdx.y * a.ychunk;
-    k.ye = (int)min(a.ny, (int64_t)k.yb + a.ychunk);
-    k.cur_col = a.cur + x * S + z * k.sz_stride + shot0;
-    k.prv_col = a.prev + x * S + z * k.sz_stride + shot0;
-    k.a_col = a.a + x + z * a.nxp;
-    k.sx = SPONGE ? __ldg(a.sx + x) : 1.f;
-    k.sz = SPONGE ? __ldg(a.sz + z) : 1.f;
-    k.gx0 = a.g[0];
-    k.gz0 = a.g[1];
-    k.gy0 = a.g[2];
-    const bool xz_in = x > 0 && x < a.nx - 1 && z > 0 && z < a.nz - 1;
-    if (!xz_in) {
-        face_column<SPL, SPONGE>(a, k);
+    k.S = a.s_pad;
+    k.zs = a.nxp * k.S;
+    k.ys = a.nxp * nz * k.S;
+    k.ays = a.nxp * nz;
+    const int64_t shot = (int64_t)blockIdx.z * 32 + lane;
+    k.cur0 = a.cur + ((int64_t)x0 + (int64_t)z * a.nxp) * k.S + shot;
+    k.prv0 = a.prev + ((int64_t)x0 + (int64_t)z * a.nxp) * k.S + shot;
+    k.a0 = a.a + x0 + (int64_t)z * a.nxp;
+    k.ny = (int)a.ny;
+    const int yb = blockIdx.y * a.ychunk;  // a multiple of O
+    k.ye = (int)min((int64_t)k.ny, (int64_t)yb + a.ychunk);
+    k.exi = exi;
+    k.last = exi == ex - 1;
+    k.lz = z % O;
+    k.szv = SPONGE ? __ldg(a.sz + z) : 1.f;
+    k.wz = cb_wa[O - 1][k.lz];
+    k.g0 = a.g[0];
+    k.g1 = a.g[1];
+    k.g2 = a.g[2];
+    float sxv[O + 1];
+#pragma unroll
+    for (int j = 0; j <= O; j++) sxv[j] = SPONGE && (j < O || k.last) ? __ldg(a.sx + x0 + j) : 1.f;
+    const bool zin = z > 0 && z < nz - 1;
+    if (!zin) {  // z-face row: every node keeps the damped previous level
+        for (int y = yb; y < k.ye; y++) {
+            const float syv = SPONGE ? __ldg(a.sy + y) : 1.f;
+#pragma unroll
+            for (int j = 0; j <= O; j++) {
+                if (j == O && !k.last) continue;
+                float *p = k.prv0 + (int64_t)y * k.ys + j * k.S;
+                const float s = SPONGE ? sxv[j] * syv * k.szv : 1.f;
+                *p = SPONGE ? s * (s * *p) : *p;
+            }
+        }
         return;
     }
-    dispatch_column<O, SPL, SPONGE>((int)(x % O), (int)(z % O), a, k);
+    float P[O + 1][O];
+    float pend[O];
+    const int e0 = yb / O;
+    if (e0 > 0) {
+#pragma unroll
+        for (int kk = 0; kk <= O; kk++)
+#pragma unroll
+            for (int j = 0; j < O; j++) P[kk][j] = __ldg(k.cur0 + (int64_t)(yb - O + kk) * k.ys + j * k.S);
+#pragma unroll
+        for (int j = 0; j < O; j++) {
+            float acc = 0.f;
+#pragma unroll
+            for (int d = -O; d <= -1; d++) acc = fmaf(Tc<O>(0, d), P[O + d][j] - P[O][j], acc);
+            pend[j] = acc;
+            P[0][j] = P[O][j];
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < O; j++) {
+            pend[j] = 0.f;
+            P[0][j] = __ldg(k.cur0 + (int64_t)yb * k.ys + j * k.S);
+        }
+    }
+    for (int y0 = e0 * O; y0 < k.ye; y0 += O) {
+#pragma unroll
+        for (int kk = 1; kk <= O; kk++)
+#pragma unroll
+            for (int j = 0; j < O; j++)
+                P[kk][j] = y0 + kk < k.ny ? __ldg(k.cur0 + (int64_t)(y0 + kk) * k.ys + j * k.S) : 0.f;
+        element_planes<O, SPONGE>(a, k, y0, sxv, P, pend);
+#pragma unroll
+        for (int j = 0; j < O; j++) {
+            float acc = 0.f;
+#pragma unroll
+            for (int d = -O; d <= -1; d++) acc = fmaf(Tc<O>(0, d), P[O + d][j] - P[O][j], acc);
+            pend[j] = acc;
+            P[0][j] = P[O][j];
+        }
+    }
 }
 
 __global__ void k_batch_source(const BatchSourceArgs a)
@@ -266,28 +269,19 @@ __global__ void k_batch_record(const BatchRecordArgs a)
     a.traces[((int64_t)step * a.nrec + r) * a.nshot + s] = a.level[a.rec_node[r] * a.s_pad + s];
 }
 
-template <int O, int SPL>
-cudaError_t launch_o(const BatchArgs &a, bool sponge, int warps_per_cta, cudaStream_t st)
+template <int O>
+cudaError_t launch_o(const BatchArgs &a0, bool sponge, int wpc, cudaStream_t st)
 {
-    const int64_t cols = a.nx * a.nz;
-    const dim3 grid((unsigned)((cols + warps_per_cta - 1) / warps_per_cta), (unsigned)((a.ny + a.ychunk - 1) / a.ychunk),
-                    (unsigned)(a.s_pad / (32 * SPL)));
-    if (sponge) k_batch<O, SPL, true><<<grid, 32 * warps_per_cta, 0, st>>>(a);
-    else k_batch<O, SPL, false><<<grid, 32 * warps_per_cta, 0, st>>>(a);
+    BatchArgs a = a0;
+    a.ychunk = (a.ychunk + O - 1) / O * O;
+    if (a.s_pad % 32) return cudaErrorInvalidValue;
+    const int ex = (int)((a.nx - 1) / O);
+    const int64_t warps = (int64_t)ex * a.nz;
+    const dim3 grid((unsigned)((warps + wpc - 1) / wpc), (unsigned)((a.ny + a.ychunk - 1) / a.ychunk),
+                    (unsigned)(a.s_pad / 32));
+    if (sponge) k_batch<O, true><<<grid, 32 * wpc, 0, st>>>(a, ex);
+    else k_batch<O, false><<<grid, 32 * wpc, 0, st>>>(a, ex);
     return cudaGetLastError();
-}
-
-template <int SPL>
-cudaError_t launch_spl(int order, const BatchArgs &a, bool sponge, int w, cudaStream_t st)
-{
-    switch (order) {
-    case 1: return launch_o<1, SPL>(a, sponge, w, st);
-    case 2: return launch_o<2, SPL>(a, sponge, w, st);
-    case 3: return launch_o<3, SPL>(a, sponge, w, st);
-    case 4: return launch_o<4, SPL>(a, sponge, w, st);
-    case 5: return launch_o<5, SPL>(a, sponge, w, st);
-    default: return cudaErrorInvalidValue;
-    }
 }
 
 }  // namespace
@@ -299,12 +293,15 @@ cudaError_t batch_kernel_setup(const float *T_all, const float *wa_all)
     return cudaMemcpyToSymbol(cb_wa, wa_all, sizeof(float) * kMaxOrder * kMaxOrder);
 }
 
-cudaError_t launch_batch_step(int order, const BatchArgs &a, bool sponge, const BatchTuning &tune, cudaStream_t st)
+cudaError_t launch_batch_step(int order, const BatchArgs &a, bool sponge, const BatchTuning &t, cudaStream_t st)
 {
-    switch (tune.shots_per_lane) {
-    case 1: return launch_spl<1>(order, a, sponge, tune.warps_per_cta, st);
-    case 2: return launch_spl<2>(order, a, sponge, tune.warps_per_cta, st);
-    case 4: return launch_spl<4>(order, a, sponge, tune.warps_per_cta, st);
+    const int wpc = t.warps_per_cta > 0 ? t.warps_per_cta : 4;
+    switch (order) {
+    case 1: return launch_o<1>(a, sponge, wpc, st);
+    case 2: return launch_o<2>(a, sponge, wpc, st);
+    case 3: return launch_o<3>(a, sponge, wpc, st);
+    case 4: return launch_o<4>(a, sponge, wpc, st);
+    case 5: return launch_o<5>(a, sponge, wpc, st);
     default: return cudaErrorInvalidValue;
     }
 }

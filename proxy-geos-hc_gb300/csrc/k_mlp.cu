@@ -1,0 +1,559 @@
+// k_mlp.cu -- kernels of the boundary network (mlp.h): BF16 tensor-core forward (mma.sync
+// m16n8k16, FP32 accumulators), the training pass (forward on the tensor cores, backward and
+// parameter gradients in FP32), Adam, and the boundary-strip gather / correction.
+//
+// Tile: 128 rows (samples or strip nodes) per CTA, 4 warps of 32 rows.  Shared memory holds the
+// BF16 weights as [out][in] rows (the MMA's column-major B operand) and the BF16 inputs and
+// hidden activations as row-major [row][in] (the row-major A operand); row strides are padded by
+// 8 elements so that the fragment loads of a warp hit 32 different banks.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "mlp.h"
+
+namespace semgb {
+
+namespace {
+
+constexpr int H = kMlpHidden;
+constexpr int KP1 = kMlpInPad + 8;  // row stride (bf16) of X and W1
+constexpr int KP2 = H + 8;          // row stride (bf16) of H1 and W2
+constexpr int T = kMlpTile;
+
+__device__ __forceinline__ uint16_t f2bf(float x)
+{
+    const __nv_bfloat16 b = __float2bfloat16_rn(x);
+    return *reinterpret_cast<const uint16_t *>(&b);
+}
+
+__device__ __forceinline__ float bf2f(uint16_t u)
+{
+    __nv_bfloat16 b;
+    *reinterpret_cast<uint16_t *>(&b) = u;
+    return __bfloat162float(b);
+}
+
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi)
+{
+    return (uint32_t)f2bf(lo) | ((uint32_t)f2bf(hi) << 16);
+}
+
+// exact GELU and its derivative
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float z)
+{
+    return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+struct NetSmem {
+    uint16_t w1[H * KP1];
+    uint16_t w2[H * KP2];
+    float b1[H], b2[H], w3[H], b3;
+};
+
+__device__ void load_net(NetSmem &s, const MlpDev &net)
+{
+    for (int i = threadIdx.x; i < H * kMlpInPad; i += blockDim.x) s.w1[(i / kMlpInPad) * KP1 + i % kMlpInPad] = net.w1[i];
+    for (int i = threadIdx.x; i < H * H; i += blockDim.x) s.w2[(i / H) * KP2 + i % H] = net.w2[i];
+    for (int i = threadIdx.x; i < H; i += blockDim.x) {
+        s.b1[i] = net.b1[i];
+        s.b2[i] = net.b2[i];
+        s.w3[i] = net.w3[i];
+    }
+    if (threadIdx.x == 0) s.b3 = net.b3[0];
+}
+
+// Forward of the warp's 32 rows (tile rows wr..wr+31): xs [T][KP1] bf16 in, h1 [T][KP2] bf16
+// written, returns y for rows wr + mt*16 + g (+8) in yv[mt][0/1] (valid on every lane of a quad).
+// With z1/z2 non-null the pre-activations are kept (FP32 [T][H]).
+__device__ void forward_rows(const NetSmem &s, const uint16_t *xs, uint16_t *h1, float *z1, float *z2, int wr,
+                             float (&yv)[2][2])
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    float acc[2][8][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[mt][nt][j] = 0.f;
+#pragma unroll
+    for (int ks = 0; ks < kMlpInPad / 16; ks++) {
+        const int k0 = ks * 16 + q * 2;
+        uint32_t a[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) {
+            const int r = wr + mt * 16 + g;
+            a[mt][0] = *reinterpret_cast<const uint32_t *>(xs + r * KP1 + k0);
+            a[mt][1] = *reinterpret_cast<const uint32_t *>(xs + (r + 8) * KP1 + k0);
+            a[mt][2] = *reinterpret_cast<const uint32_t *>(xs + r * KP1 + k0 + 8);
+            a[mt][3] = *reinterpret_cast<const uint32_t *>(xs + (r + 8) * KP1 + k0 + 8);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            const int n = nt * 8 + g;
+            uint32_t b[2];
+            b[0] = *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0);
+            b[1] = *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0 + 8);
+            mma16816(acc[0][nt], a[0], b);
+            mma16816(acc[1][nt], a[1], b);
+        }
+    }
+    // layer-1 epilogue: bias, GELU, BF16 into h1 (the warp's own rows)
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            const int c = nt * 8 + q * 2;
+#pragma unroll
+            for (int hrow = 0; hrow < 2; hrow++) {
+                const int r = wr + mt * 16 + g + hrow * 8;
+                const float za = acc[mt][nt][hrow * 2] + s.b1[c], zb = acc[mt][nt][hrow * 2 + 1] + s.b1[c + 1];
+                if (z1) {
+                    z1[r * H + c] = za;
+                    z1[r * H + c + 1] = zb;
+                }
+                *reinterpret_cast<uint32_t *>(h1 + r * KP2 + c) = pack_bf2(gelu(za), gelu(zb));
+                acc[mt][nt][hrow * 2] = 0.f;
+                acc[mt][nt][hrow * 2 + 1] = 0.f;
+            }
+        }
+    __syncwarp();
+#pragma unroll
+    for (int ks = 0; ks < H / 16; ks++) {
+        const int k0 = ks * 16 + q * 2;
+        uint32_t a[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) {
+            const int r = wr + mt * 16 + g;
+            a[mt][0] = *reinterpret_cast<const uint32_t *>(h1 + r * KP2 + k0);
+            a[mt][1] = *reinterpret_cast<const uint32_t *>(h1 + (r + 8) * KP2 + k0);
+            a[mt][2] = *reinterpret_cast<const uint32_t *>(h1 + r * KP2 + k0 + 8);
+            a[mt][3] = *reinterpret_cast<const uint32_t *>(h1 + (r + 8) * KP2 + k0 + 8);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            const int n = nt * 8 + g;
+            uint32_t b[2];
+            b[0] = *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0);
+            b[1] = *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0 + 8);
+            mma16816(acc[0][nt], a[0], b);
+            mma16816(acc[1][nt], a[1], b);
+        }
+    }
+    // layer-2 epilogue and the output layer: y = b3 + sum_c w3[c] GELU(z2[c])
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int hrow = 0; hrow < 2; hrow++) {
+            const int r = wr + mt * 16 + g + hrow * 8;
+            float part = 0.f;
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                const int c = nt * 8 + q * 2;
+                const float za = acc[mt][nt][hrow * 2] + s.b2[c], zb = acc[mt][nt][hrow * 2 + 1] + s.b2[c + 1];
+                if (z2) {
+                    z2[r * H + c] = za;
+                    z2[r * H + c + 1] = zb;
+                }
+                part = fmaf(s.w3[c], gelu(za), part);
+                part = fmaf(s.w3[c + 1], gelu(zb), part);
+            }
+            part += __shfl_xor_sync(0xffffffffu, part, 1);
+            part += __shfl_xor_sync(0xffffffffu, part, 2);
+            yv[mt][hrow] = part + s.b3;
+        }
+}
+
+// stage rows [row0, row0 + T) of x [n][81] (FP32, scaled by 1/scale[i] when scale is given) as
+// BF16 [T][KP1] with zero padding
+__device__ void stage_x(uint16_t *xs, const float *x, int64_t row0, int64_t n)
+{
+    for (int i = threadIdx.x; i < T * kMlpInPad; i += blockDim.x) {
+        const int r = i / kMlpInPad, k = i - r * kMlpInPad;
+        const int64_t row = row0 + r;
+        const float v = (row < n && k < kMlpIn) ? x[row * kMlpIn + k] : 0.f;
+        xs[r * KP1 + k] = f2bf(v);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_mlp_forward(const MlpDev net, const float *x, float *y, int64_t n)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
+    uint16_t *xs = reinterpret_cast<uint16_t *>(smem + sizeof(NetSmem));
+    uint16_t *h1 = xs + T * KP1;
+    load_net(s, net);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    for (int64_t row0 = (int64_t)blockIdx.x * T; row0 < n; row0 += (int64_t)gridDim.x * T) {
+        __syncthreads();
+        stage_x(xs, x, row0, n);
+        __syncthreads();
+        float yv[2][2];
+        forward_rows(s, xs, h1, nullptr, nullptr, w * 32, yv);
+        if (q == 0)
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int hrow = 0; hrow < 2; hrow++) {
+                    const int64_t row = row0 + w * 32 + mt * 16 + g + hrow * 8;
+                    if (row < n) y[row] = yv[mt][hrow];
+                }
+    }
+}
+
+// Training pass: loss and parameter gradients over all n samples, accumulated per CTA in shared
+// memory (each gradient entry owned by one thread) and added to the global buffers once.
+struct TrainSmem {
+    float z1[T * H];
+    float z2[T * H];
+    float dy[T];
+    float g[kMlpParams];
+};
+
+__global__ void __launch_bounds__(128) k_mlp_train_pass(const MlpDev net, const float *x, const float *t, int64_t n,
+                                                        double *loss, float *grad)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
+    uint16_t *xs = reinterpret_cast<uint16_t *>(smem + sizeof(NetSmem));
+    uint16_t *h1 = xs + T * KP1;
+    TrainSmem &ts = *reinterpret_cast<TrainSmem *>(h1 + T * KP2);
+    load_net(s, net);
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) ts.g[i] = 0.f;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    const int tid = threadIdx.x;
+    const float inv_n = 1.f / (float)n;
+    double lsum = 0.0;
+    for (int64_t row0 = (int64_t)blockIdx.x * T; row0 < n; row0 += (int64_t)gridDim.x * T) {
+        __syncthreads();
+        stage_x(xs, x, row0, n);
+        __syncthreads();
+        float yv[2][2];
+        forward_rows(s, xs, h1, ts.z1, ts.z2, w * 32, yv);
+        if (q == 0)
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int hrow = 0; hrow < 2; hrow++) {
+                    const int r = w * 32 + mt * 16 + g + hrow * 8;
+                    const int64_t row = row0 + r;
+                    float d = 0.f;
+                    if (row < n) {
+                        const float e = yv[mt][hrow] - t[row];
+                        lsum += (double)e * e;
+                        d = 2.f * e * inv_n;
+                    }
+                    ts.dy[r] = d;
+                }
+        __syncthreads();
+        // row pass (thread = row): output layer, dZ2 = dy w3 GELU'(z2) in place of z2
+        {
+            const int r = tid;
+            const float d = ts.dy[r];
+            for (int c = 0; c < H; c++) {
+                const float z = ts.z2[r * H + c];
+                ts.z2[r * H + c] = d * s.w3[c] * gelu_d(z);
+            }
+        }
+        __syncthreads();
+        // column sums: db2[c] (thread c < 64) and db3; dw3 needs GELU(z2), which this pass
+        // overwrites, so k_mlp_grad_w3 accumulates it from a second forward
+        if (tid < H) {
+            float a2 = 0.f;
+            for (int r = 0; r < T; r++) a2 += ts.z2[r * H + tid];
+            ts.g[kOffB2 + tid] += a2;
+        } else if (tid == H) {
+            float a = 0.f;
+            for (int r = 0; r < T; r++) a += ts.dy[r];
+            ts.g[kOffB3] += a;
+        }
+        // dW2[n][k] = sum_r dZ2[r][n] H1[r][k]: 4096 entries, 32 per thread
+        for (int e = tid; e < H * H; e += blockDim.x) {
+            const int nn = e / H, k = e - nn * H;
+            float a = 0.f;
+            for (int r = 0; r < T; r++) a = fmaf(ts.z2[r * H + nn], bf2f(h1[r * KP2 + k]), a);
+            ts.g[kOffW2 + e] += a;
+        }
+        __syncthreads();
+        // row pass: dZ1[r][k] = GELU'(z1[r][k]) sum_n dZ2[r][n] W2[n][k], in place of z1
+        {
+            const int r = tid;
+            float dh[H];
+#pragma unroll
+            for (int k = 0; k < H; k++) dh[k] = 0.f;
+            for (int nn = 0; nn < H; nn++) {
+                const float dz = ts.z2[r * H + nn];
+#pragma unroll
+                for (int k = 0; k < H; k++) dh[k] = fmaf(dz, bf2f(s.w2[nn * KP2 + k]), dh[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < H; k++) ts.z1[r * H + k] = dh[k] * gelu_d(ts.z1[r * H + k]);
+        }
+        __syncthreads();
+        // db1 and dW1[n][k] = sum_r dZ1[r][n] X[r][k] (k < 81)
+        if (tid < H) {
+            float a = 0.f;
+            for (int r = 0; r < T; r++) a += ts.z1[r * H + tid];
+            ts.g[kOffB1 + tid] += a;
+        }
+        for (int e = tid; e < H * kMlpIn; e += blockDim.x) {
+            const int nn = e / kMlpIn, k = e - nn * kMlpIn;
+            float a = 0.f;
+            for (int r = 0; r < T; r++) a = fmaf(ts.z1[r * H + nn], bf2f(xs[r * KP1 + k]), a);
+            ts.g[kOffW1 + e] += a;
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x)
+        if (ts.g[i] != 0.f) atomicAdd(grad + i, ts.g[i]);
+    // loss: quad leaders hold partial sums
+    lsum += __shfl_xor_sync(0xffffffffu, lsum, 4);
+    lsum += __shfl_xor_sync(0xffffffffu, lsum, 8);
+    lsum += __shfl_xor_sync(0xffffffffu, lsum, 16);
+    if (lane == 0) atomicAdd(loss, lsum / (double)n);
+}
+
+// dw3[c] = sum_r dy[r] GELU(z2[r][c]) needs the forward activations the training pass
+// overwrites; this pass recomputes them (forward only) and accumulates dw3.
+__global__ void __launch_bounds__(128) k_mlp_grad_w3(const MlpDev net, const float *x, const float *t, int64_t n,
+                                                     float *grad)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
+    uint16_t *xs = reinterpret_cast<uint16_t *>(smem + sizeof(NetSmem));
+    uint16_t *h1 = xs + T * KP1;
+    float *z2 = reinterpret_cast<float *>(h1 + T * KP2);
+    float *dy = z2 + T * H;
+    float *gw3 = dy + T;
+    load_net(s, net);
+    for (int i = threadIdx.x; i < H; i += blockDim.x) gw3[i] = 0.f;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    const float inv_n = 1.f / (float)n;
+    for (int64_t row0 = (int64_t)blockIdx.x * T; row0 < n; row0 += (int64_t)gridDim.x * T) {
+        __syncthreads();
+        stage_x(xs, x, row0, n);
+        __syncthreads();
+        float yv[2][2];
+        forward_rows(s, xs, h1, nullptr, z2, w * 32, yv);
+        if (q == 0)
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int hrow = 0; hrow < 2; hrow++) {
+                    const int r = w * 32 + mt * 16 + g + hrow * 8;
+                    const int64_t row = row0 + r;
+                    dy[r] = row < n ? 2.f * (yv[mt][hrow] - t[row]) * inv_n : 0.f;
+                }
+        __syncthreads();
+        if (threadIdx.x < H) {
+            const int c = threadIdx.x;
+            float a = 0.f;
+            for (int r = 0; r < T; r++) a = fmaf(dy[r], gelu(z2[r * H + c]), a);
+            gw3[c] += a;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < H; i += blockDim.x) atomicAdd(grad + kOffW3 + i, gw3[i]);
+}
+
+__global__ void k_mlp_pack(const float *m, uint16_t *w1, uint16_t *w2, float *b1, float *b2, float *w3, float *b3)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < H * kMlpInPad) {
+        const int nn = i / kMlpInPad, k = i - nn * kMlpInPad;
+        w1[i] = f2bf(k < kMlpIn ? m[kOffW1 + nn * kMlpIn + k] : 0.f);
+    }
+    if (i < H * H) w2[i] = f2bf(m[kOffW2 + i]);
+    if (i < H) {
+        b1[i] = m[kOffB1 + i];
+        b2[i] = m[kOffB2 + i];
+        w3[i] = m[kOffW3 + i];
+    }
+    if (i == 0) b3[0] = m[kOffB3];
+}
+
+__global__ void k_mlp_adam(float *p, const float *g, float *m, float *v, float lr, float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kMlpParams) return;
+    const float gi = g[i];
+    const float mi = 0.9f * m[i] + 0.1f * gi;
+    const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + 1e-8f);
+}
+
+// ---- boundary strip ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const AbcArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
+    uint16_t *xs = reinterpret_cast<uint16_t *>(smem + sizeof(NetSmem));
+    uint16_t *h1 = xs + T * KP1;
+    float *scale = reinterpret_cast<float *>(h1 + T * KP2);
+    float *xf = scale + T;  // [T][81] FP32 features before scaling
+    load_net(s, net);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    const int64_t plane = a.nxp * a.nz;
+    for (int64_t row0 = (int64_t)blockIdx.x * T; row0 < a.n; row0 += (int64_t)gridDim.x * T) {
+        __syncthreads();
+        // gather: feature (level l, neighbour (dz, dy, dx)) -> l*27 + (dz+1)*9 + (dy+1)*3 + (dx+1)
+        for (int i = threadIdx.x; i < T * kMlpIn; i += blockDim.x) {
+            const int r = i / kMlpIn, f = i - r * kMlpIn;
+            const int64_t row = row0 + r;
+            float v = 0.f;
+            if (row < a.n) {
+                const int l = f / 27, nb = f - l * 27;
+                const int dz = nb / 9 - 1, dy = (nb / 3) % 3 - 1, dx = nb % 3 - 1;
+                const int64_t q0 = a.nodes[row];
+                const int64_t iy = q0 / plane, rr = q0 - iy * plane, iz = rr / a.nxp, ix = rr - iz * a.nxp;
+                const int64_t jx = ix + dx, jy = iy + dy, jz = iz + dz;
+                if (jx >= 0 && jx < a.nx && jy >= 0 && jy < a.ny && jz >= 0 && jz < a.nz) {
+                    const int64_t qj = jx + jz * a.nxp + jy * plane;
+                    if (l == 0) v = a.p_new[qj];
+                    else if (l == 1) v = a.p_cur[qj] * (a.sx ? (a.sx[jx] * a.sy[jy]) * a.sz[jz] : 1.f);
+                    else v = a.hist[qj];
+                }
+            }
+            xf[r * kMlpIn + f] = v;
+        }
+        __syncthreads();
+        {
+            const int r = threadIdx.x;  // one row per thread (128 threads)
+            float m = 0.f;
+            for (int f = 0; f < kMlpIn; f++) m = fmaxf(m, fabsf(xf[r * kMlpIn + f]));
+            scale[r] = m + 1e-30f;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < T * kMlpInPad; i += blockDim.x) {
+            const int r = i / kMlpInPad, k = i - r * kMlpInPad;
+            xs[r * KP1 + k] = f2bf(k < kMlpIn ? xf[r * kMlpIn + k] / scale[r] : 0.f);
+        }
+        __syncthreads();
+        float yv[2][2];
+        forward_rows(s, xs, h1, nullptr, nullptr, w * 32, yv);
+        if (q == 0)
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int hrow = 0; hrow < 2; hrow++) {
+                    const int r = w * 32 + mt * 16 + g + hrow * 8;
+                    const int64_t row = row0 + r;
+                    if (row < a.n) a.corr[row] = scale[r] * yv[mt][hrow];
+                }
+    }
+}
+
+__global__ void k_abc_apply(const AbcArgs a, float *p_new)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x)
+        p_new[a.nodes[i]] += a.corr[i];
+}
+
+// hist <- p^n (actual values) on the history shell
+__global__ void k_abc_history(const int64_t *shell, int64_t n, const float *p_cur, const float *sx, const float *sy,
+                              const float *sz, int64_t nxp, int64_t nz, float *hist)
+{
+    const int64_t plane = nxp * nz;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q0 = shell[i];
+        const int64_t iy = q0 / plane, rr = q0 - iy * plane, iz = rr / nxp, ix = rr - iz * nxp;
+        hist[q0] = p_cur[q0] * (sx ? (sx[ix] * sy[iy]) * sz[iz] : 1.f);
+    }
+}
+
+size_t smem_forward() { return sizeof(NetSmem) + sizeof(uint16_t) * T * (KP1 + KP2); }
+size_t smem_train() { return smem_forward() + sizeof(TrainSmem); }
+size_t smem_w3() { return smem_forward() + sizeof(float) * (T * H + T + H); }
+size_t smem_abc() { return smem_forward() + sizeof(float) * (T + T * kMlpIn); }
+
+int grid_for(int64_t n)
+{
+    const int64_t tiles = (n + T - 1) / T;
+    return (int)std::min<int64_t>(tiles, 152 * 4);
+}
+
+}  // namespace
+
+cudaError_t mlp_pack(const float *master, uint16_t *w1, uint16_t *w2, float *b1, float *b2, float *w3, float *b3,
+                     cudaStream_t s)
+{
+    k_mlp_pack<<<(H * kMlpInPad + 255) / 256, 256, 0, s>>>(master, w1, w2, b1, b2, w3, b3);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_forward(const MlpDev &net, const float *x, float *y, int64_t n, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const size_t sm = smem_forward();
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_mlp_forward<<<grid_for(n), T, sm, s>>>(net, x, y, n);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_loss_grad(const MlpDev &net, const float *x, const float *t, int64_t n, double *loss, float *grad,
+                          cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    size_t sm = smem_train();
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_train_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_mlp_train_pass<<<grid_for(n), T, sm, s>>>(net, x, t, n, loss, grad);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    sm = smem_w3();
+    if ((e = cudaFuncSetAttribute(k_mlp_grad_w3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
+        return e;
+    k_mlp_grad_w3<<<grid_for(n), T, sm, s>>>(net, x, t, n, grad);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_adam(float *master, const float *grad, float *m, float *v, int t, float lr, cudaStream_t s)
+{
+    const float c1 = 1.f / (1.f - powf(0.9f, (float)t)), c2 = 1.f / (1.f - powf(0.999f, (float)t));
+    k_mlp_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(master, grad, m, v, lr, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t abc_correction(const MlpDev &net, const AbcArgs &a, cudaStream_t s)
+{
+    if (a.n <= 0) return cudaSuccess;
+    const size_t sm = smem_abc();
+    cudaError_t e = cudaFuncSetAttribute(k_abc_correction, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_abc_correction<<<grid_for(a.n), T, sm, s>>>(net, a);
+    return cudaGetLastError();
+}
+
+cudaError_t abc_apply(const AbcArgs &a, float *p_new, float *hist, cudaStream_t s)
+{
+    (void)hist;
+    if (a.n > 0) k_abc_apply<<<(int)std::min<int64_t>((a.n + 255) / 256, 152 * 16), 256, 0, s>>>(a, p_new);
+    return cudaGetLastError();
+}
+
+cudaError_t abc_history(const int64_t *shell, int64_t n, const float *p_cur, const float *sx, const float *sy,
+                        const float *sz, int64_t nxp, int64_t nz, float *hist, cudaStream_t s)
+{
+    if (n > 0)
+        k_abc_history<<<(int)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(shell, n, p_cur, sx, sy, sz,
+                                                                                         nxp, nz, hist);
+    return cudaGetLastError();
+}
+
+}  // namespace semgb

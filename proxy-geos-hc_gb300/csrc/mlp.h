@@ -1,0 +1,63 @@
+// mlp.h -- the boundary network of the learned absorbing boundary: 81 inputs (p at three time
+// levels on the 3x3x3 node neighbourhood, divided by a per-node scale), two hidden layers of 64
+// with GELU, one output.  BF16 weights and activations into FP32 accumulators on the tensor
+// cores (mma.sync m16n8k16), FP32 master weights and Adam state for training.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace semgb {
+
+constexpr int kMlpIn = 81;
+constexpr int kMlpInPad = 96;  // K of layer 1 padded to whole 16-wide MMA steps
+constexpr int kMlpHidden = 64;
+// FP32 master layout: W1[64][81], b1[64], W2[64][64], b2[64], w3[64], b3
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kMlpHidden * kMlpIn;
+constexpr int kOffW2 = kOffB1 + kMlpHidden;
+constexpr int kOffB2 = kOffW2 + kMlpHidden * kMlpHidden;
+constexpr int kOffW3 = kOffB2 + kMlpHidden;
+constexpr int kOffB3 = kOffW3 + kMlpHidden;
+constexpr int kMlpParams = kOffB3 + 1;
+constexpr int kMlpTile = 128;  // rows (nodes or samples) per CTA
+
+// Device copy of the network for the kernels: BF16 W1 as [64][96] (zero-padded K) and W2 as
+// [64][64], FP32 biases and output layer.
+struct MlpDev {
+    const uint16_t *w1;  // [64][96] bf16 bits
+    const uint16_t *w2;  // [64][64]
+    const float *b1, *b2, *w3, *b3;
+};
+
+// Strip of nodes the network corrects, and the levels it reads.
+struct AbcArgs {
+    const int64_t *nodes;  // device-layout indices of the strip nodes
+    int64_t n;
+    const float *p_new;    // p^{n+1} (sponge applied)
+    const float *p_cur;    // p^n stored without its last sponge factor (actual = s * stored)
+    const float *hist;     // p^{n-1} (actual values) on the history shell, device layout [n_int]
+    const float *sx, *sy, *sz;  // sponge factors (null: none)
+    int64_t nx, nxp, ny, nz;
+    float *corr;           // out: correction per strip node
+};
+
+// bf16 conversion of the FP32 master weights into the device layout.
+cudaError_t mlp_pack(const float *master, uint16_t *w1, uint16_t *w2, float *b1, float *b2, float *w3, float *b3,
+                     cudaStream_t s);
+// y[i] = net(x[i]) for x [n][81] (FP32, device).
+cudaError_t mlp_forward(const MlpDev &net, const float *x, float *y, int64_t n, cudaStream_t s);
+// Loss 1/n sum (net(x_i) - t_i)^2 accumulated into *loss (double), gradients with respect to the
+// master parameters accumulated into grad (FP32 [kMlpParams]).
+cudaError_t mlp_loss_grad(const MlpDev &net, const float *x, const float *t, int64_t n, double *loss, float *grad,
+                          cudaStream_t s);
+// Adam step on the FP32 master weights (m, v moments; t = step count starting at 1).
+cudaError_t mlp_adam(float *master, const float *grad, float *m, float *v, int t, float lr, cudaStream_t s);
+// Boundary correction: corr[i] = scale_i * net(features_i / scale_i) for the strip nodes.
+cudaError_t abc_correction(const MlpDev &net, const AbcArgs &a, cudaStream_t s);
+// p_new[node_i] += corr[i].
+cudaError_t abc_apply(const AbcArgs &a, float *p_new, float *hist, cudaStream_t s);
+// hist[q] <- p^n (actual: stored value times the node's sponge factor) on the history shell.
+cudaError_t abc_history(const int64_t *shell, int64_t n, const float *p_cur, const float *sx, const float *sy,
+                        const float *sz, int64_t nxp, int64_t nz, float *hist, cudaStream_t s);
+
+}  // namespace semgb

@@ -87,6 +87,12 @@ _SIGS = {
     "sem_batch_get_pressure": [_VP, C.c_int, C.c_int, _F32P],
     "sem_batch_time_step": [_VP, C.c_int, _F32P],
     "sem_batch_autotune": [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "sem_traces_write": [C.c_char_p, C.c_int, C.c_int, _F32P, C.c_float, _F32P, C.c_int, _F32P, C.c_char_p],
+    "sem_traces_read_info": [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)],
+    "sem_traces_read": [C.c_char_p, _F32P],
+    "sem_solver_write_snapshot": [_VP, C.c_int, C.c_int, C.c_char_p],
+    "sem_snapshot_read_info": [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "sem_snapshot_read": [C.c_char_p, _F32P],
     "sem_group_create": [C.c_int, C.POINTER(_VP), C.POINTER(_VP)],
     "sem_group_destroy": [_VP],
     "sem_group_step": [_VP, C.c_int],
@@ -329,10 +335,43 @@ class Solver:
     def synchronize(self):
         _check(lib().sem_solver_synchronize(self._h))
 
+    def write_snapshot(self, path, level: int = LEVEL_CURRENT, y_index: int = -1):
+        """One x-z plane of a level to a SEMSNP01 container (y_index -1: ny/2 - 1)."""
+        _check(lib().sem_solver_write_snapshot(self._h, level, y_index, str(path).encode()))
+
     def time_kernels(self, n: int) -> np.ndarray:
         ms = np.zeros(3, np.float32)
         _check(lib().sem_solver_time_kernels(self._h, n, _p(ms, _F32P)))
         return ms
+
+
+def write_traces(path, traces, dt, rec_xyz=None, src_xyz=None, extra_json=None):
+    """Write traces [n_steps][n_rec] to a SEMTRC01 container (sem_traces_write)."""
+    t = _f32(traces)
+    ns, nr = t.shape
+    r = _f32(rec_xyz).reshape(nr, 3) if rec_xyz is not None else None
+    s = _f32(src_xyz).reshape(-1, 3) if src_xyz is not None else np.zeros((0, 3), np.float32)
+    _check(lib().sem_traces_write(str(path).encode(), ns, nr, _p(t, _F32P), dt,
+                                  _p(r, _F32P) if r is not None else None, len(s), _p(s, _F32P),
+                                  extra_json.encode() if extra_json else None))
+
+
+def read_traces(path):
+    """Traces [n_steps][n_rec] and dt from a SEMTRC01 container (sem_traces_read)."""
+    ns, nr, dt = C.c_int(), C.c_int(), C.c_float()
+    _check(lib().sem_traces_read_info(str(path).encode(), C.byref(ns), C.byref(nr), C.byref(dt)))
+    out = np.zeros((ns.value, nr.value), np.float32)
+    _check(lib().sem_traces_read(str(path).encode(), _p(out, _F32P)))
+    return out, dt.value
+
+
+def read_snapshot(path):
+    """(plane [nz][nx], y_index) from a SEMSNP01 container (sem_snapshot_read)."""
+    nx, nz, y = C.c_int(), C.c_int(), C.c_int()
+    _check(lib().sem_snapshot_read_info(str(path).encode(), C.byref(nx), C.byref(nz), C.byref(y)))
+    out = np.zeros((nz.value, nx.value), np.float32)
+    _check(lib().sem_snapshot_read(str(path).encode(), _p(out, _F32P)))
+    return out, y.value
 
 
 def solver_from_workload(wl, kernel: int = KERNEL_AUTO):
