@@ -312,6 +312,55 @@ int sem_element_step_noalloc(int ex, int ey, int ez, float lx, float ly, float l
                              const float *sx, const float *sy, const float *sz, void *stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Learned absorbing boundary.  The reference has none (its only sponge is the FD proxy's,
+ * FDTDinit.hpp:319-396).  A small network corrects, after every step, the new level on the
+ * boundary nodes (layer_elems 0: the network gives the new face values, which the Dirichlet
+ * update would hold fixed) or on the interior nodes within `layer_elems` elements of a face
+ * (a correction added to the new level) -- the "strip" --
+ * from p^{n+1}, p^n and
+ * p^{n-1} on each node's 3x3x3 neighbourhood: 81 features divided by their largest magnitude,
+ * two hidden layers of 64 with GELU, one output clipped to [-1, 1] and multiplied back by that
+ * magnitude.  BF16 weights
+ * and activations, FP32 accumulation on the tensor cores; FP32 master weights for training.
+ * Parameter layout (sem_mlp_n_params floats): W1[64][81], b1[64], W2[64][64], b2[64], w3[64], b3.
+ * ------------------------------------------------------------------------------------------ */
+
+typedef struct sem_mlp sem_mlp;
+typedef struct sem_abc sem_abc;
+
+int sem_mlp_create(uint64_t seed, sem_mlp **out);
+int sem_mlp_destroy(sem_mlp *net);
+int sem_mlp_n_params(void);
+int sem_mlp_set_params(sem_mlp *net, const float *params);
+int sem_mlp_get_params(sem_mlp *net, float *params);
+/* y[i] = net(x[i]), x [n][81] (host). */
+int sem_mlp_forward(sem_mlp *net, int64_t n, const float *x, float *y);
+/* Mean squared error over n samples and its gradient with respect to the parameters (host
+ * arrays); the rounding to BF16 is passed through as the identity. */
+int sem_mlp_loss_grad(sem_mlp *net, int64_t n, const float *x, const float *t, double *loss, float *grad);
+/* Adam (beta 0.9 / 0.999) on minibatches of `batch` samples for `epochs` passes over the
+ * samples (shuffled with `seed`); losses[epoch] = mean minibatch loss (may be NULL). */
+int sem_mlp_train(sem_mlp *net, int64_t n, const float *x, const float *t, int epochs, int batch, float lr,
+                  uint64_t seed, double *losses);
+
+/* Attach `net` to a solver (stencil pass) for the strip of `layer_elems` elements. */
+int sem_abc_create(sem_solver *s, sem_mlp *net, int layer_elems, sem_abc **out);
+int sem_abc_destroy(sem_abc *a);
+/* Strip nodes and history nodes (strip plus its inner neighbour layer). */
+int sem_abc_info(const sem_abc *a, int64_t *n_nodes, int64_t *n_history);
+int sem_abc_nodes(const sem_abc *a, int64_t *nodes); /* reference numbering, [n_nodes] */
+/* n_steps solver steps, each followed by the correction (enqueued on the solver's stream). */
+int sem_abc_step(sem_abc *a, int n_steps);
+/* The correction alone, for the step that just ran (as sem_abc_step applies it). */
+int sem_abc_correct(sem_abc *a);
+/* Zero the p^{n-1} history, or set it from a full level (n_nodes floats, actual values). */
+int sem_abc_reset(sem_abc *a);
+int sem_abc_set_history(sem_abc *a, const float *p_prev);
+/* The network inputs of every strip node for the step that just ran: x [n_nodes][81] already
+ * divided by scale [n_nodes] (may be NULL), as the correction kernel forms them. */
+int sem_abc_features(sem_abc *a, float *x, float *scale);
+
+/* ------------------------------------------------------------------------------------------
  * Output formats.  One container for traces and snapshots: 8-byte magic, little-endian uint64
  * header length, UTF-8 JSON header, zero padding to a 64-byte boundary, little-endian float32
  * samples.  Traces ("SEMTRC01") are stored trace-major (SEG-Y's order: each receiver's whole

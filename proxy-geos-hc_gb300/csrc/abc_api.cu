@@ -1,0 +1,434 @@
+// abc_api.cu -- C ABI of the learned absorbing boundary: the boundary network (sem_mlp_*) and
+// its attachment to a solver (sem_abc_*).
+//
+// After every solver step the network corrects the new level on the strip nodes -- the boundary
+// nodes themselves (layer 0), or the interior nodes within `layer` elements of a face -- from
+// p^{n+1}, p^n and p^{n-1} on each node's 3x3x3
+// neighbourhood (81 features, divided by their largest magnitude; the output, clipped to [-1, 1],
+// is multiplied back).  On the boundary nodes it is the node's new value (so it never exceeds
+// the largest magnitude of its neighbourhood), on interior strip nodes a correction.
+// p^{n-1} of the strip and of its inner neighbour layer is kept in a history array.  The
+// sponge of the solver (if any) still applies; the network replaces most of its thickness.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <random>
+#include <vector>
+
+#include "abi.h"
+#include "mlp.h"
+#include "solver.h"
+
+using namespace semgb;
+
+struct sem_mlp {
+    float *d_master = nullptr;  // FP32 parameters (mlp.h layout)
+    float *d_m = nullptr, *d_v = nullptr, *d_grad = nullptr;
+    uint16_t *d_w1 = nullptr, *d_w2 = nullptr;
+    float *d_b1 = nullptr, *d_b2 = nullptr, *d_w3 = nullptr, *d_b3 = nullptr;
+    double *d_loss = nullptr;
+    int adam_t = 0;
+    cudaStream_t stream = nullptr;
+    MlpDev dev() const { return MlpDev{d_w1, d_w2, d_b1, d_b2, d_w3, d_b3}; }
+};
+
+struct sem_abc {
+    sem_solver *s = nullptr;
+    sem_mlp *net = nullptr;
+    int layer = 0;
+    int64_t *d_nodes = nullptr;  // strip nodes (device layout)
+    int64_t n = 0;
+    int64_t *d_shell = nullptr;  // history nodes: strip and its inner neighbours
+    int64_t n_shell = 0;
+    float *d_hist = nullptr;     // [n_int]
+    float *d_corr = nullptr;     // [n]
+};
+
+namespace {
+
+int net_upload(sem_mlp *m)
+{
+    CUDA_TRY(mlp_pack(m->d_master, m->d_w1, m->d_w2, m->d_b1, m->d_b2, m->d_w3, m->d_b3, m->stream));
+    CUDA_TRY(cudaStreamSynchronize(m->stream));
+    return SEM_OK;
+}
+
+AbcArgs abc_args(const sem_abc *a)
+{
+    const sem_solver *s = a->s;
+    const Box &b = s->mesh->box;
+    AbcArgs x{};
+    x.nodes = a->d_nodes;
+    x.n = a->n;
+    x.p_new = s->d_p[s->cur];      // after a step the new level is the current one
+    x.p_cur = s->d_p[1 - s->cur];  // and p^n the stored previous one
+    x.hist = a->d_hist;
+    x.sx = s->sponge ? s->d_sx : nullptr;
+    x.sy = s->sponge ? s->d_sy : nullptr;
+    x.sz = s->sponge ? s->d_sz : nullptr;
+    x.nx = b.nx;
+    x.nxp = b.nxp;
+    x.ny = b.ny;
+    x.nz = b.nz;
+    x.corr = a->d_corr;
+    x.absolute = a->layer == 0 ? 1 : 0;
+    return x;
+}
+
+// correction after the step that just ran (levels as abc_args reads them)
+cudaError_t enqueue_correction(sem_abc *a)
+{
+    sem_solver *s = a->s;
+    const AbcArgs x = abc_args(a);
+    cudaError_t e = abc_correction(a->net->dev(), x, s->stream);
+    if (e != cudaSuccess) return e;
+    if ((e = abc_apply(x, s->d_p[s->cur], a->d_hist, s->stream)) != cudaSuccess) return e;
+    const Box &b = s->mesh->box;
+    return abc_history(a->d_shell, a->n_shell, s->d_p[1 - s->cur], x.sx, x.sy, x.sz, b.nxp, b.nz, a->d_hist,
+                       s->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- network -------------------------------------------------------------------------------
+
+int sem_mlp_destroy(sem_mlp *m)
+{
+    if (!m) return SEM_OK;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    dfree(m->d_master); dfree(m->d_m); dfree(m->d_v); dfree(m->d_grad);
+    dfree(m->d_w1); dfree(m->d_w2); dfree(m->d_b1); dfree(m->d_b2); dfree(m->d_w3); dfree(m->d_b3);
+    dfree(m->d_loss);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return SEM_OK;
+}
+
+int sem_mlp_create(uint64_t seed, sem_mlp **out)
+{
+    GUARD_BEGIN
+    if (!out) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    sem_mlp *m = new sem_mlp();
+    cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = dalloc(&m->d_master, kMlpParams);
+    if (e == cudaSuccess) e = dalloc(&m->d_m, kMlpParams);
+    if (e == cudaSuccess) e = dalloc(&m->d_v, kMlpParams);
+    if (e == cudaSuccess) e = dalloc(&m->d_grad, kMlpParams);
+    if (e == cudaSuccess) e = dalloc(&m->d_w1, kMlpHidden * kMlpInPad);
+    if (e == cudaSuccess) e = dalloc(&m->d_w2, kMlpHidden * kMlpHidden);
+    if (e == cudaSuccess) e = dalloc(&m->d_b1, kMlpHidden);
+    if (e == cudaSuccess) e = dalloc(&m->d_b2, kMlpHidden);
+    if (e == cudaSuccess) e = dalloc(&m->d_w3, kMlpHidden);
+    if (e == cudaSuccess) e = dalloc(&m->d_b3, 1);
+    if (e == cudaSuccess) e = dalloc(&m->d_loss, 1);
+    if (e != cudaSuccess) {
+        sem_mlp_destroy(m);
+        return sem_fail(SEM_ERR_OOM, cudaGetErrorString(e));
+    }
+    // He-normal hidden layers, a small output layer (the initial correction is close to zero)
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<float> nd(0.f, 1.f);
+    std::vector<float> p(kMlpParams, 0.f);
+    for (int i = 0; i < kMlpHidden * kMlpIn; i++) p[kOffW1 + i] = nd(rng) * std::sqrt(2.f / kMlpIn);
+    for (int i = 0; i < kMlpHidden * kMlpHidden; i++) p[kOffW2 + i] = nd(rng) * std::sqrt(2.f / kMlpHidden);
+    for (int i = 0; i < kMlpHidden; i++) p[kOffW3 + i] = nd(rng) * 0.01f;
+    int rc = sem_mlp_set_params(m, p.data());
+    if (rc) {
+        sem_mlp_destroy(m);
+        return rc;
+    }
+    *out = m;
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_mlp_n_params(void) { return kMlpParams; }
+
+int sem_mlp_set_params(sem_mlp *m, const float *params)
+{
+    GUARD_BEGIN
+    if (!m || !params) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    for (int i = 0; i < kMlpParams; i++)
+        if (!std::isfinite(params[i])) return sem_fail(SEM_ERR_ARG, "non-finite parameter");
+    CUDA_TRY(cudaMemcpy(m->d_master, params, kMlpParams * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(m->d_m, 0, kMlpParams * 4));
+    CUDA_TRY(cudaMemset(m->d_v, 0, kMlpParams * 4));
+    m->adam_t = 0;
+    return net_upload(m);
+    GUARD_END
+}
+
+int sem_mlp_get_params(sem_mlp *m, float *params)
+{
+    GUARD_BEGIN
+    if (!m || !params) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    CUDA_TRY(cudaStreamSynchronize(m->stream));
+    CUDA_TRY(cudaMemcpy(params, m->d_master, kMlpParams * 4, cudaMemcpyDeviceToHost));
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_mlp_forward(sem_mlp *m, int64_t n, const float *x, float *y)
+{
+    GUARD_BEGIN
+    if (!m || n < 0 || (n > 0 && (!x || !y))) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    if (n == 0) return SEM_OK;
+    float *dx = nullptr, *dy = nullptr;
+    CUDA_TRY(dalloc(&dx, (size_t)n * kMlpIn));
+    cudaError_t e = dalloc(&dy, (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, (size_t)n * kMlpIn * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = mlp_forward(m->dev(), dx, dy, n, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(y, dy, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    dfree(dx);
+    dfree(dy);
+    CUDA_TRY(e);
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_mlp_loss_grad(sem_mlp *m, int64_t n, const float *x, const float *t, double *loss, float *grad)
+{
+    GUARD_BEGIN
+    if (!m || n < 1 || !x || !t) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    float *dx = nullptr, *dt = nullptr;
+    CUDA_TRY(dalloc(&dx, (size_t)n * kMlpIn));
+    cudaError_t e = dalloc(&dt, (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, (size_t)n * kMlpIn * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dt, t, (size_t)n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->d_grad, 0, kMlpParams * 4, m->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->d_loss, 0, 8, m->stream);
+    if (e == cudaSuccess) e = mlp_loss_grad(m->dev(), dx, dt, n, m->d_loss, m->d_grad, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    if (e == cudaSuccess && loss) e = cudaMemcpy(loss, m->d_loss, 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && grad) e = cudaMemcpy(grad, m->d_grad, kMlpParams * 4, cudaMemcpyDeviceToHost);
+    dfree(dx);
+    dfree(dt);
+    CUDA_TRY(e);
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_mlp_train(sem_mlp *m, int64_t n, const float *x, const float *t, int epochs, int batch, float lr,
+                  uint64_t seed, double *losses)
+{
+    GUARD_BEGIN
+    if (!m || n < 1 || !x || !t || epochs < 0 || batch < 1 || !(lr > 0))
+        return sem_fail(SEM_ERR_ARG, "bad arguments");
+    // samples resident on the device, shuffled once per epoch on the host (index order)
+    float *dx = nullptr, *dt = nullptr, *bx = nullptr, *bt = nullptr;
+    const int64_t nb = std::min<int64_t>(batch, n);
+    CUDA_TRY(dalloc(&dx, (size_t)n * kMlpIn));
+    cudaError_t e = dalloc(&dt, (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&bx, (size_t)nb * kMlpIn);
+    if (e == cudaSuccess) e = dalloc(&bt, (size_t)nb);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, (size_t)n * kMlpIn * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dt, t, (size_t)n * 4, cudaMemcpyHostToDevice);
+    std::vector<int64_t> perm(n);
+    for (int64_t i = 0; i < n; i++) perm[i] = i;
+    int64_t *dperm = nullptr;
+    if (e == cudaSuccess) e = dalloc(&dperm, (size_t)n);
+    std::mt19937_64 rng(seed);
+    for (int ep = 0; ep < epochs && e == cudaSuccess; ep++) {
+        std::shuffle(perm.begin(), perm.end(), rng);
+        e = cudaMemcpyAsync(dperm, perm.data(), (size_t)n * 8, cudaMemcpyHostToDevice, m->stream);
+        double lsum = 0.0;
+        int64_t seen = 0;
+        for (int64_t b0 = 0; b0 + nb <= n && e == cudaSuccess; b0 += nb) {
+            e = mlp_gather_rows(dx, dt, dperm + b0, nb, bx, bt, m->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(m->d_grad, 0, kMlpParams * 4, m->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(m->d_loss, 0, 8, m->stream);
+            if (e == cudaSuccess) e = mlp_loss_grad(m->dev(), bx, bt, nb, m->d_loss, m->d_grad, m->stream);
+            if (e == cudaSuccess) e = mlp_adam(m->d_master, m->d_grad, m->d_m, m->d_v, ++m->adam_t, lr, m->stream);
+            if (e == cudaSuccess)
+                e = mlp_pack(m->d_master, m->d_w1, m->d_w2, m->d_b1, m->d_b2, m->d_w3, m->d_b3, m->stream);
+            double l = 0;
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&l, m->d_loss, 8, cudaMemcpyDeviceToHost, m->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+            lsum += l * nb;
+            seen += nb;
+        }
+        if (losses) losses[ep] = seen ? lsum / seen : 0.0;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    dfree(dx); dfree(dt); dfree(bx); dfree(bt); dfree(dperm);
+    CUDA_TRY(e);
+    return SEM_OK;
+    GUARD_END
+}
+
+// ---- boundary ------------------------------------------------------------------------------
+
+int sem_abc_destroy(sem_abc *a)
+{
+    if (!a) return SEM_OK;
+    if (a->s) cudaStreamSynchronize(a->s->stream);
+    dfree(a->d_nodes);
+    dfree(a->d_shell);
+    dfree(a->d_hist);
+    dfree(a->d_corr);
+    delete a;
+    return SEM_OK;
+}
+
+int sem_abc_create(sem_solver *s, sem_mlp *net, int layer_elems, sem_abc **out)
+{
+    GUARD_BEGIN
+    if (!s || !net || !out) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    const Box &b = s->mesh->box;
+    if (layer_elems < 0 || 2 * layer_elems > std::min({b.ex, b.ey, b.ez}))
+        return sem_fail(SEM_ERR_ARG, "layer must be >= 0 elements and fit twice in every axis");
+    // layer 0: the boundary nodes themselves (the network supplies the face values that the
+    // Dirichlet update would hold fixed); layer w > 0: interior nodes within w elements of a face
+    const int64_t w = (int64_t)layer_elems * b.order;
+    std::vector<int64_t> nodes, shell;
+    for (int64_t iy = 0; iy < b.ny; iy++)
+        for (int64_t iz = 0; iz < b.nz; iz++)
+            for (int64_t ix = 0; ix < b.nx; ix++) {
+                const int64_t d = std::min({ix, b.nx - 1 - ix, iy, b.ny - 1 - iy, iz, b.nz - 1 - iz});
+                const int64_t q = ix + iz * b.nxp + iy * b.nxp * b.nz;
+                if (w == 0 ? d == 0 : (d >= 1 && d <= w)) nodes.push_back(q);
+                if (d <= w + 1) shell.push_back(q);
+            }
+    sem_abc *a = new sem_abc();
+    a->s = s;
+    a->net = net;
+    a->layer = layer_elems;
+    a->n = (int64_t)nodes.size();
+    a->n_shell = (int64_t)shell.size();
+    cudaError_t e = dalloc(&a->d_nodes, nodes.size());
+    if (e == cudaSuccess) e = dalloc(&a->d_shell, shell.size());
+    if (e == cudaSuccess) e = dalloc(&a->d_hist, (size_t)b.n_int);
+    if (e == cudaSuccess) e = dalloc(&a->d_corr, nodes.size());
+    if (e == cudaSuccess) e = cudaMemcpy(a->d_nodes, nodes.data(), nodes.size() * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(a->d_shell, shell.data(), shell.size() * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(a->d_hist, 0, (size_t)b.n_int * 4);
+    if (e != cudaSuccess) {
+        sem_abc_destroy(a);
+        return sem_fail(SEM_ERR_OOM, cudaGetErrorString(e));
+    }
+    *out = a;
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_abc_info(const sem_abc *a, int64_t *n_nodes, int64_t *n_history)
+{
+    if (!a) return sem_fail(SEM_ERR_ARG, "NULL boundary");
+    if (n_nodes) *n_nodes = a->n;
+    if (n_history) *n_history = a->n_shell;
+    return SEM_OK;
+}
+
+int sem_abc_nodes(const sem_abc *a, int64_t *nodes)
+{
+    GUARD_BEGIN
+    if (!a || !nodes) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    std::vector<int64_t> q(a->n);
+    CUDA_TRY(cudaMemcpy(q.data(), a->d_nodes, a->n * 8, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < a->n; i++) nodes[i] = to_reference(a->s->mesh->box, q[i]);
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_abc_reset(sem_abc *a)
+{
+    GUARD_BEGIN
+    if (!a) return sem_fail(SEM_ERR_ARG, "NULL boundary");
+    CUDA_TRY(cudaStreamSynchronize(a->s->stream));
+    CUDA_TRY(cudaMemset(a->d_hist, 0, (size_t)a->s->mesh->box.n_int * 4));
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_abc_set_history(sem_abc *a, const float *p_prev)
+{
+    GUARD_BEGIN
+    if (!a || !p_prev) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    const Box &b = a->s->mesh->box;
+    CUDA_TRY(cudaStreamSynchronize(a->s->stream));
+    CUDA_TRY(cudaMemcpy2D(a->d_hist, b.nxp * 4, p_prev, b.nx * 4, b.nx * 4, b.nz * b.ny, cudaMemcpyHostToDevice));
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_abc_step(sem_abc *a, int n_steps)
+{
+    GUARD_BEGIN
+    if (!a || n_steps < 0) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    if (n_steps == 0) return SEM_OK;
+    sem_solver *s = a->s;
+    if (s->kernel == SEM_KERNEL_ELEMENT) return sem_fail(SEM_ERR_STATE, "the learned boundary runs with the stencil pass");
+    int rc = solver_prepare(s, n_steps);
+    if (rc) return rc;
+    for (int k = 0; k < n_steps; k++) {
+        CUDA_TRY(solver_enqueue_step(s, s->cur));
+        s->cur ^= 1;
+        CUDA_TRY(enqueue_correction(a));
+    }
+    s->steps_done += n_steps;
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_abc_correct(sem_abc *a)
+{
+    GUARD_BEGIN
+    if (!a) return sem_fail(SEM_ERR_ARG, "NULL boundary");
+    CUDA_TRY(enqueue_correction(a));
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_abc_features(sem_abc *a, float *x, float *scale)
+{
+    GUARD_BEGIN
+    if (!a || !x) return sem_fail(SEM_ERR_ARG, "NULL argument");
+    // the features exactly as k_abc_correction gathers them (same order, sponge product and
+    // scaling), from host copies of the levels: training sets are built from these
+    sem_solver *s = a->s;
+    const Box &b = s->mesh->box;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    std::vector<float> pn(b.n_int), pc(b.n_int), ph(b.n_int);
+    CUDA_TRY(cudaMemcpy(pn.data(), s->d_p[s->cur], b.n_int * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(pc.data(), s->d_p[1 - s->cur], b.n_int * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(ph.data(), a->d_hist, b.n_int * 4, cudaMemcpyDeviceToHost));
+    std::vector<float> sx(b.nx, 1.f), sy(b.ny, 1.f), sz(b.nz, 1.f);
+    if (s->sponge) {
+        CUDA_TRY(cudaMemcpy(sx.data(), s->d_sx, b.nx * 4, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(sy.data(), s->d_sy, b.ny * 4, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(sz.data(), s->d_sz, b.nz * 4, cudaMemcpyDeviceToHost));
+    }
+    std::vector<int64_t> q(a->n);
+    CUDA_TRY(cudaMemcpy(q.data(), a->d_nodes, a->n * 8, cudaMemcpyDeviceToHost));
+    const int64_t plane = b.nxp * b.nz;
+    for (int64_t i = 0; i < a->n; i++) {
+        const int64_t iy = q[i] / plane, rr = q[i] - iy * plane, iz = rr / b.nxp, ix = rr - iz * b.nxp;
+        float m = 0.f;
+        float *f = x + i * kMlpIn;
+        for (int l = 0; l < 3; l++)
+            for (int nb = 0; nb < 27; nb++) {
+                const int dz = nb / 9 - 1, dy = (nb / 3) % 3 - 1, dx = nb % 3 - 1;
+                const int64_t jx = ix + dx, jy = iy + dy, jz = iz + dz;
+                float v = 0.f;
+                if (jx >= 0 && jx < b.nx && jy >= 0 && jy < b.ny && jz >= 0 && jz < b.nz) {
+                    const int64_t qj = jx + jz * b.nxp + jy * plane;
+                    v = l == 0 ? pn[qj] : l == 1 ? pc[qj] * ((sx[jx] * sy[jy]) * sz[jz]) : ph[qj];
+                }
+                f[l * 27 + nb] = v;
+                m = std::max(m, std::fabs(v));
+            }
+        const float sc = m + 1e-30f;
+        for (int k = 0; k < kMlpIn; k++) f[k] /= sc;
+        if (scale) scale[i] = sc;
+    }
+    return SEM_OK;
+    GUARD_END
+}
+
+}  // extern "C"

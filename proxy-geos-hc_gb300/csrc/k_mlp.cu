@@ -454,7 +454,14 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
                 for (int hrow = 0; hrow < 2; hrow++) {
                     const int r = w * 32 + mt * 16 + g + hrow * 8;
                     const int64_t row = row0 + r;
-                    if (row < a.n) a.corr[row] = scale[r] * yv[mt][hrow];
+                    // the features are normalised by their largest magnitude: a correction larger
+                    // than that is clipped (it bounds what one step of the network can inject)
+                    if (row < a.n) {
+                        const float v = scale[r] * fminf(fmaxf(yv[mt][hrow], -1.f), 1.f);
+                        // absolute: the new value itself, which then never exceeds the largest
+                        // magnitude of its own neighbourhood over the three levels
+                        a.corr[row] = a.absolute ? v - a.p_new[a.nodes[row]] : v;
+                    }
                 }
     }
 }
@@ -474,6 +481,17 @@ __global__ void k_abc_history(const int64_t *shell, int64_t n, const float *p_cu
         const int64_t q0 = shell[i];
         const int64_t iy = q0 / plane, rr = q0 - iy * plane, iz = rr / nxp, ix = rr - iz * nxp;
         hist[q0] = p_cur[q0] * (sx ? (sx[ix] * sy[iy]) * sz[iz] : 1.f);
+    }
+}
+
+__global__ void k_gather_rows(const float *x, const float *t, const int64_t *idx, int64_t nb, float *bx, float *bt)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb * kMlpIn;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / kMlpIn, k = i - r * kMlpIn;
+        const int64_t src = idx[r];
+        bx[i] = x[src * kMlpIn + k];
+        if (k == 0) bt[r] = t[src];
     }
 }
 
@@ -527,6 +545,14 @@ cudaError_t mlp_adam(float *master, const float *grad, float *m, float *v, int t
 {
     const float c1 = 1.f / (1.f - powf(0.9f, (float)t)), c2 = 1.f / (1.f - powf(0.999f, (float)t));
     k_mlp_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(master, grad, m, v, lr, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_gather_rows(const float *x, const float *t, const int64_t *idx, int64_t nb, float *bx, float *bt,
+                            cudaStream_t s)
+{
+    if (nb > 0)
+        k_gather_rows<<<(int)std::min<int64_t>((nb * kMlpIn + 255) / 256, 152 * 16), 256, 0, s>>>(x, t, idx, nb, bx, bt);
     return cudaGetLastError();
 }
 

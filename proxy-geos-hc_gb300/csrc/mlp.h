@@ -39,6 +39,7 @@ struct AbcArgs {
     const float *sx, *sy, *sz;  // sponge factors (null: none)
     int64_t nx, nxp, ny, nz;
     float *corr;           // out: correction per strip node
+    int absolute;          // 1: the network gives the node's value (scale * y), 0: a correction
 };
 
 // bf16 conversion of the FP32 master weights into the device layout.
@@ -50,6 +51,9 @@ cudaError_t mlp_forward(const MlpDev &net, const float *x, float *y, int64_t n, 
 // master parameters accumulated into grad (FP32 [kMlpParams]).
 cudaError_t mlp_loss_grad(const MlpDev &net, const float *x, const float *t, int64_t n, double *loss, float *grad,
                           cudaStream_t s);
+// bx[i] = x[idx[i]], bt[i] = t[idx[i]] for i < nb (minibatch rows).
+cudaError_t mlp_gather_rows(const float *x, const float *t, const int64_t *idx, int64_t nb, float *bx, float *bt,
+                            cudaStream_t s);
 // Adam step on the FP32 master weights (m, v moments; t = step count starting at 1).
 cudaError_t mlp_adam(float *master, const float *grad, float *m, float *v, int t, float lr, cudaStream_t s);
 // Boundary correction: corr[i] = scale_i * net(features_i / scale_i) for the strip nodes.

@@ -87,6 +87,23 @@ _SIGS = {
     "sem_batch_get_pressure": [_VP, C.c_int, C.c_int, _F32P],
     "sem_batch_time_step": [_VP, C.c_int, _F32P],
     "sem_batch_autotune": [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "sem_mlp_create": [C.c_uint64, C.POINTER(_VP)],
+    "sem_mlp_destroy": [_VP],
+    "sem_mlp_n_params": [],
+    "sem_mlp_set_params": [_VP, _F32P],
+    "sem_mlp_get_params": [_VP, _F32P],
+    "sem_mlp_forward": [_VP, C.c_int64, _F32P, _F32P],
+    "sem_mlp_loss_grad": [_VP, C.c_int64, _F32P, _F32P, _F64P, _F32P],
+    "sem_mlp_train": [_VP, C.c_int64, _F32P, _F32P, C.c_int, C.c_int, C.c_float, C.c_uint64, _F64P],
+    "sem_abc_create": [_VP, _VP, C.c_int, C.POINTER(_VP)],
+    "sem_abc_destroy": [_VP],
+    "sem_abc_info": [_VP, _I64P, _I64P],
+    "sem_abc_nodes": [_VP, _I64P],
+    "sem_abc_step": [_VP, C.c_int],
+    "sem_abc_correct": [_VP],
+    "sem_abc_reset": [_VP],
+    "sem_abc_set_history": [_VP, _F32P],
+    "sem_abc_features": [_VP, _F32P, _F32P],
     "sem_traces_write": [C.c_char_p, C.c_int, C.c_int, _F32P, C.c_float, _F32P, C.c_int, _F32P, C.c_char_p],
     "sem_traces_read_info": [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)],
     "sem_traces_read": [C.c_char_p, _F32P],
@@ -503,6 +520,115 @@ class Group:
         ms = C.c_float()
         _check(lib().sem_group_time_step(self._h, n, C.byref(ms)))
         return ms.value
+
+
+class Mlp:
+    """The boundary network (sem_mlp_*): 81 -> 64 -> 64 -> 1, GELU, BF16 weights on the tensor
+    cores with FP32 accumulation, FP32 master parameters and Adam."""
+
+    N_IN = 81
+
+    def __init__(self, seed: int = 0):
+        h = _VP()
+        _check(lib().sem_mlp_create(seed, C.byref(h)))
+        self._h = h
+        self.n_params = lib().sem_mlp_n_params()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sem_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, np.float32)
+        _check(lib().sem_mlp_get_params(self._h, _p(out, _F32P)))
+        return out
+
+    @params.setter
+    def params(self, p):
+        v = _f32(p).reshape(-1)
+        assert v.size == self.n_params
+        _check(lib().sem_mlp_set_params(self._h, _p(v, _F32P)))
+
+    def forward(self, x):
+        x = _f32(x).reshape(-1, self.N_IN)
+        y = np.zeros(len(x), np.float32)
+        _check(lib().sem_mlp_forward(self._h, len(x), _p(x, _F32P), _p(y, _F32P)))
+        return y
+
+    def loss_grad(self, x, t):
+        x = _f32(x).reshape(-1, self.N_IN)
+        t = _f32(t).reshape(-1)
+        loss = C.c_double()
+        g = np.zeros(self.n_params, np.float32)
+        _check(lib().sem_mlp_loss_grad(self._h, len(x), _p(x, _F32P), _p(t, _F32P), C.byref(loss), _p(g, _F32P)))
+        return loss.value, g
+
+    def train(self, x, t, epochs, batch=4096, lr=1e-3, seed=0):
+        x = _f32(x).reshape(-1, self.N_IN)
+        t = _f32(t).reshape(-1)
+        losses = np.zeros(max(epochs, 1), np.float64)
+        _check(lib().sem_mlp_train(self._h, len(x), _p(x, _F32P), _p(t, _F32P), epochs, batch, lr, seed,
+                                   _p(losses, _F64P)))
+        return losses[:epochs]
+
+
+class Abc:
+    """Learned absorbing boundary on a solver (sem_abc_*): after every step the network corrects
+    the new level on the interior nodes within `layer` elements of a face."""
+
+    def __init__(self, solver: Solver, net: Mlp, layer: int = 1):
+        h = _VP()
+        _check(lib().sem_abc_create(solver._h, net._h, layer, C.byref(h)))
+        self._h = h
+        self.solver = solver
+        self.net = net
+        n, m = C.c_int64(), C.c_int64()
+        _check(lib().sem_abc_info(h, C.byref(n), C.byref(m)))
+        self.n_nodes = n.value
+        self.n_history = m.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sem_abc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def nodes(self):
+        out = np.zeros(self.n_nodes, np.int64)
+        _check(lib().sem_abc_nodes(self._h, _p(out, _I64P)))
+        return out
+
+    def step(self, n=1):
+        _check(lib().sem_abc_step(self._h, n))
+
+    def correct(self):
+        _check(lib().sem_abc_correct(self._h))
+
+    def reset(self):
+        _check(lib().sem_abc_reset(self._h))
+
+    def set_history(self, p_prev):
+        v = _f32(p_prev)
+        _check(lib().sem_abc_set_history(self._h, _p(v, _F32P)))
+
+    def features(self):
+        x = np.zeros((self.n_nodes, Mlp.N_IN), np.float32)
+        sc = np.zeros(self.n_nodes, np.float32)
+        _check(lib().sem_abc_features(self._h, _p(x, _F32P), _p(sc, _F32P)))
+        return x, sc
 
 
 class Adjoint:

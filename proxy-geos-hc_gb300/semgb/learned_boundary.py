@@ -1,0 +1,211 @@
+"""Learned absorbing boundary: training data from padded-domain runs, training, evaluation.
+
+A truncated problem (mesh T: the region of interest plus a thin sponge) and a padded problem
+(mesh P: the same region with `pad` extra elements on every side, its own sponge far away) share
+the element size, order, velocity and source.  The padded run gives the reflection-free field
+on T's nodes.
+
+Training data (teacher forcing): at every step n, T's levels are set to the padded run's
+(p^n, p^{n-1}) on T's nodes, T takes one plain step, and each strip node contributes the
+network inputs of that step (sem_abc_features) with the target p_P^{n+1} / scale on boundary
+nodes (the face value of the padded run) or (p_P^{n+1} - p_T^{n+1}) / scale on interior strip
+nodes (the correction that would have reproduced the padded run).
+
+Evaluation: T runs from rest with and without the network; the reflected energy is
+sum over steps and interior nodes (the strip excluded) of (p_T - p_P)^2, divided by the same sum
+of p_P^2.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import LEVEL_CURRENT, LEVEL_PREVIOUS, KERNEL_STENCIL, Abc, Mesh, Mlp, Solver, ricker
+
+
+@dataclass
+class Setup:
+    ex: int                  # elements per axis of the truncated mesh T
+    order: int
+    h: float
+    c: float                 # velocity (m/s)
+    pad: int                 # extra elements per side of the padded mesh P
+    sponge_t: int            # sponge of T (elements)
+    sponge_p: int            # sponge of P (elements)
+    layer: int               # strip of the network (elements; 0: the boundary nodes)
+    f0: float
+    dt: float
+    steps: int
+    src_frac: tuple = (0.5, 0.5, 0.5)  # source position as a fraction of T's box
+    sigma: float = 0.06
+
+    @property
+    def nx_t(self):
+        return self.ex * self.order + 1
+
+    @property
+    def off(self):
+        return self.pad * self.order
+
+
+def _solver(s: Setup, ne: int, sponge: int, shift: float):
+    L = ne * s.h
+    mesh = Mesh(ne, ne, ne, L, L, L, s.order)
+    mesh.set_velocity(np.full(ne ** 3, s.c, np.float32))
+    sol = Solver(mesh, s.dt)
+    sol.set_kernel(KERNEL_STENCIL)
+    if sponge > 0:
+        sol.set_sponge(sponge, s.sigma)
+    Lt = s.ex * s.h
+    xyz = np.array([[shift + f * Lt for f in s.src_frac]], np.float32)
+    sol.set_source_points(xyz, ricker(s.steps + 2, s.dt, s.f0, 1)[None])
+    return mesh, sol
+
+
+def make_solvers(s: Setup):
+    """(mesh_T, solver_T), (mesh_P, solver_P) with the source at the same physical point."""
+    return _solver(s, s.ex, s.sponge_t, 0.0), _solver(s, s.ex + 2 * s.pad, s.sponge_p, s.pad * s.h)
+
+
+def restrict(s: Setup, field_p):
+    """Field of mesh P (reference numbering) restricted to T's nodes."""
+    n_p = (s.ex + 2 * s.pad) * s.order + 1
+    f = np.asarray(field_p).reshape(n_p, n_p, n_p)  # [y][z][x]
+    o, n = s.off, s.nx_t
+    return np.ascontiguousarray(f[o:o + n, o:o + n, o:o + n]).reshape(-1)
+
+
+def _target(s: Setup, ref, plain):
+    """Network target before the division by the scale: the padded run's value on boundary nodes
+    (layer 0), the correction from T's plain update to it on interior strip nodes."""
+    return ref if s.layer == 0 else ref - plain
+
+
+def teacher_forced_samples(s: Setup, per_step: int = 4000, seed: int = 0, min_rel_scale: float = 1e-4):
+    """(x [N][81], t [N]) from the padded run, `per_step` strip nodes sampled per step among
+    those whose field is not negligible."""
+    rng = np.random.default_rng(seed)
+    (mt, st), (mp, sp) = make_solvers(s)
+    net0 = Mlp(seed)  # not used for the plain step; Abc needs one to gather features
+    abc = Abc(st, net0, s.layer)
+    strip = abc.nodes()
+    xs, ts = [], []
+    smax = 0.0
+    for n in range(s.steps):
+        pc = restrict(s, sp.pressure(LEVEL_CURRENT))
+        pq = restrict(s, sp.pressure(LEVEL_PREVIOUS))
+        st.set_pressure(LEVEL_CURRENT, pc)
+        st.set_pressure(LEVEL_PREVIOUS, pq)
+        abc.set_history(pq)
+        st.step(1)
+        sp.step(1)
+        x, sc = abc.features()
+        target = _target(s, restrict(s, sp.pressure(LEVEL_CURRENT))[strip], st.pressure(LEVEL_CURRENT)[strip])
+        smax = max(smax, float(sc.max()))
+        keep = np.nonzero(sc > min_rel_scale * max(smax, 1e-30))[0]
+        if len(keep) == 0:
+            continue
+        pick = rng.choice(keep, min(per_step, len(keep)), replace=False)
+        xs.append(x[pick])
+        ts.append((target[pick] / sc[pick]).astype(np.float32))
+    for o in (abc, net0, st, sp, mt, mp):
+        o.close()
+    if not xs:
+        return np.zeros((0, Mlp.N_IN), np.float32), np.zeros(0, np.float32)
+    return np.concatenate(xs), np.concatenate(ts)
+
+
+def rollout_samples(s: Setup, net: Mlp, per_step: int = 4000, seed: int = 0, min_rel_scale: float = 1e-4,
+                    blowup: float = 1e3):
+    """(x, t) from a run of T with the network (the states the method itself produces): at every
+    step the target is the correction that would bring T's new level on the strip to the padded
+    run's, from T's own plain update.  Stops early if T's field exceeds `blowup` times the padded
+    run's largest value."""
+    rng = np.random.default_rng(seed)
+    (mt, st), (mp, sp) = make_solvers(s)
+    abc = Abc(st, net, s.layer)
+    strip = abc.nodes()
+    xs, ts = [], []
+    smax = 0.0
+    pmax = 1e-30
+    for n in range(s.steps):
+        st.step(1)
+        sp.step(1)
+        x, sc = abc.features()
+        ref = restrict(s, sp.pressure(LEVEL_CURRENT))
+        pmax = max(pmax, float(np.abs(ref).max()))
+        target = _target(s, ref[strip], st.pressure(LEVEL_CURRENT)[strip])
+        smax = max(smax, float(sc.max()))
+        if smax > blowup * pmax:
+            break
+        keep = np.nonzero(sc > min_rel_scale * max(smax, 1e-30))[0]
+        if len(keep):
+            pick = rng.choice(keep, min(per_step, len(keep)), replace=False)
+            xs.append(x[pick])
+            ts.append(np.clip(target[pick] / sc[pick], -1.0, 1.0).astype(np.float32))
+        abc.correct()
+    for o in (abc, st, sp, mt, mp):
+        o.close()
+    if not xs:
+        return np.zeros((0, Mlp.N_IN), np.float32), np.zeros(0, np.float32)
+    return np.concatenate(xs), np.concatenate(ts)
+
+
+def train_network(s: Setup, net: Mlp, rounds: int = 3, epochs: int = 12, per_step: int = 3000, batch: int = 2048,
+                  lr: float = 1e-3, seed: int = 0):
+    """Teacher-forced samples first, then `rounds` rounds of samples from runs with the current
+    network, each followed by training on everything gathered so far.  Returns the per-round
+    sample counts and final losses."""
+    xs, ts = [], []
+    x, t = teacher_forced_samples(s, per_step, seed)
+    xs.append(x)
+    ts.append(np.clip(t, -1.0, 1.0))
+    log = []
+    for r in range(rounds + 1):
+        X, Tt = np.concatenate(xs), np.concatenate(ts)
+        losses = net.train(X, Tt, epochs=epochs, batch=batch, lr=lr, seed=seed + r)
+        log.append({"round": r, "samples": int(len(X)), "loss": float(losses[-1]) if len(losses) else None})
+        if r < rounds:
+            x, t = rollout_samples(s, net, per_step, seed + 100 + r)
+            xs.append(x)
+            ts.append(t)
+    return log
+
+
+def interior_mask(s: Setup):
+    """T's nodes outside the strip and the sponge (reference numbering)."""
+    n = s.nx_t
+    w = max(s.layer, s.sponge_t, 1) * s.order
+    i = np.arange(n)
+    a = (i > w) & (i < n - 1 - w)
+    return (a[:, None, None] & a[None, :, None] & a[None, None, :]).reshape(-1)
+
+
+def reflected_energy(s: Setup, net: Mlp | None, sample_every: int = 4):
+    """Reflected energy of T (with the network when given) against the padded run, over the
+    interior of T; also the wall time per step of T's time loop."""
+    (mt, st), (mp, sp) = make_solvers(s)
+    abc = Abc(st, net, s.layer) if net is not None else None
+    mask = interior_mask(s)
+    num = den = 0.0
+    t_loop = 0.0
+    for n0 in range(0, s.steps, sample_every):
+        k = min(sample_every, s.steps - n0)
+        t0 = time.perf_counter()
+        if abc is not None:
+            abc.step(k)
+        else:
+            st.step(k)
+        st.synchronize()
+        t_loop += time.perf_counter() - t0
+        sp.step(k)
+        ref = restrict(s, sp.pressure(LEVEL_CURRENT))[mask].astype(np.float64)
+        got = st.pressure(LEVEL_CURRENT)[mask].astype(np.float64)
+        num += float(np.sum((got - ref) ** 2))
+        den += float(np.sum(ref ** 2))
+    for o in (abc, st, sp, mt, mp):
+        if o is not None:
+            o.close()
+    return num / max(den, 1e-300), t_loop / s.steps

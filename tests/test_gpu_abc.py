@@ -1,0 +1,128 @@
+"""Learned absorbing boundary: the network's GPU kernels (BF16 tensor-core forward, training pass)
+against the CPU oracle, the strip correction against the oracle on the solver's own features, a
+zero network reproducing the plain solver, and the trained network reducing the reflected energy
+of the same thin sponge."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _params(seed, scale=0.3):
+    rng = np.random.default_rng(seed)
+    p = rng.standard_normal(M.N_PARAMS) * scale
+    return p.astype(np.float32)
+
+
+def test_forward_matches_oracle(semgb_lib, cuda_device):
+    semgb = semgb_lib
+    net = semgb.Mlp(1)
+    p = _params(2)
+    net.params = p
+    x = np.random.default_rng(3).uniform(-1, 1, (1000, 81)).astype(np.float32)
+    y = net.forward(x)
+    yo, _ = M.forward(p, x)
+    assert rel_l2(y, yo) < 2e-3
+
+
+def test_loss_and_gradient_match_oracle(semgb_lib, cuda_device):
+    semgb = semgb_lib
+    net = semgb.Mlp(1)
+    p = _params(4, 0.2)
+    net.params = p
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, (777, 81)).astype(np.float32)  # not a multiple of the 128-row tile
+    t = rng.standard_normal(777).astype(np.float32)
+    loss, g = net.loss_grad(x, t)
+    lo, go = M.loss_grad(p, x, t)
+    assert abs(loss - lo) <= 2e-3 * lo
+    assert rel_l2(g, go) < 5e-3
+    for name, (a, b) in {"W1": (0, 64 * 81), "W2": (64 * 81 + 64, 64 * 81 + 64 + 4096)}.items():
+        assert rel_l2(g[a:b], go[a:b]) < 5e-3, name
+
+
+def test_training_reduces_loss(semgb_lib, cuda_device):
+    semgb = semgb_lib
+    net = semgb.Mlp(7)
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-1, 1, (20000, 81)).astype(np.float32)
+    t = (np.tanh(x[:, :27].sum(1) * 0.3) - 0.2 * x[:, 40]).astype(np.float32)
+    l0, _ = net.loss_grad(x, t)
+    losses = net.train(x, t, epochs=15, batch=1024, lr=2e-3, seed=1)
+    l1, _ = net.loss_grad(x, t)
+    assert l1 < 0.05 * l0, (l0, l1, losses)
+
+
+def _solver(semgb, wl):
+    mesh, s = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
+    return mesh, s
+
+
+def test_zero_network_is_the_plain_step(semgb_lib, cuda_device):
+    semgb = semgb_lib
+    from semgb import workloads as W
+    wl = W.small_random(8, 7, 6, 3, 40, seed=31, nsrc=1, nrec=6)
+    m1, plain = _solver(semgb, wl)
+    plain.step(40)
+    m2, s = _solver(semgb, wl)
+    net = semgb.Mlp(0)
+    net.params = np.zeros(net.n_params, np.float32)
+    abc = semgb.Abc(s, net, 1)
+    abc.step(40)
+    assert np.array_equal(s.pressure(), plain.pressure())
+    assert np.array_equal(s.traces(), plain.traces())
+
+
+def test_strip_correction_matches_oracle(semgb_lib, cuda_device):
+    semgb = semgb_lib
+    from semgb import workloads as W
+    wl = W.small_random(8, 8, 8, 2, 30, seed=32, nsrc=1, nrec=4)
+    mesh, s = _solver(semgb, wl)
+    net = semgb.Mlp(0)
+    p = _params(9, 0.05)
+    net.params = p
+    abc = semgb.Abc(s, net, 2)
+    abc.step(29)  # fields reach the strip; history filled by the corrections
+    s.step(1)     # one plain step; the correction for it is applied below
+    x, sc = abc.features()
+    nodes = abc.nodes()
+    before = s.pressure()
+    abc.correct()
+    got = s.pressure()[nodes] - before[nodes]
+    yo, _ = M.forward(p, x)
+    want = sc * yo
+    big = np.abs(want) > 1e-3 * np.abs(want).max()
+    assert big.sum() > 100
+    assert rel_l2(got[big], want[big]) < 5e-3
+    # only the strip changes
+    other = np.ones(mesh.n_nodes, bool)
+    other[nodes] = False
+    assert np.array_equal(s.pressure()[other], before[other])
+
+
+def test_trained_network_reduces_reflections(semgb_lib, cuda_device):
+    """Thin sponge (2 elements) with and without the trained network on the boundary nodes,
+    against a padded run: the network lowers the reflected energy in the interior."""
+    semgb = semgb_lib
+    from semgb import learned_boundary as LB
+    from semgb import workloads as W
+    c, h, o = 2000.0, 10.0, 4
+    dt = W.cfl_dt(h, o, c)
+    s = LB.Setup(ex=10, order=o, h=h, c=c, pad=10, sponge_t=2, sponge_p=6, layer=0, f0=40.0, dt=dt, steps=260,
+                 src_frac=(0.35, 0.5, 0.5))
+    net = semgb.Mlp(3)
+    log = LB.train_network(s, net, rounds=2, epochs=10, per_step=3000, seed=0)
+    print(log)
+    assert log[0]["samples"] > 50000
+    e_plain, _ = LB.reflected_energy(s, None)
+    e_net, _ = LB.reflected_energy(s, net)
+    print(f"reflected energy: sponge only {e_plain:.3e}, sponge + network {e_net:.3e}")
+    assert e_net < 0.8 * e_plain
