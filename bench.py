@@ -341,7 +341,8 @@ def run_ours(args):
             s.close()
             mesh.close()
             torch.cuda.synchronize()
-            line["rows"] = {"batched": measure_batched(), "uneven": measure_uneven(), "adjoint": measure_adjoint()}
+            line["rows"] = {"batched": measure_batched(), "uneven": measure_uneven(), "adjoint": measure_adjoint(),
+                            "learned_boundary": measure_learned()}
         print(json.dumps(line), flush=True)
     s.close()
     mesh.close()
@@ -496,6 +497,58 @@ def measure_adjoint(shots: int = 2, fd_dirs: int = 2, n: int = 96, steps: int = 
             "Gnode_steps_per_s": 3 * N * steps / t_grad / 1e9,
             "note": "3 passes per gradient: forward with checkpoints, recompute with K.p recorded, adjoint",
             "fd_checks": checks}
+
+
+def measure_learned(steps_time: int = 40):
+    """Learned absorbing boundary.  Quality on a small region of interest (6^3 Q4 elements): the
+    network (trained here, on the boundary nodes of a 3-element sponge) against the same sponge
+    alone and a 20-element sponge, reflected energy against a padded run.  Speed at the 120^3
+    size: 120^3 Q4 with a 20-element sponge (region of interest 80^3) against 86^3 Q4 with a
+    3-element sponge and the network, ms per step of each time loop (CUDA events)."""
+    import torch
+    import semgb
+    from semgb import learned_boundary as LB
+    from semgb import workloads as W
+    c, h, o = 2000.0, 10.0, 4
+    dt = W.cfl_dt(h, o, c)
+    common = dict(interior=6, order=o, h=h, c=c, sponge_p=6, f0=40.0, dt=dt, steps=260, src_frac=(0.25, 0.5, 0.5))
+    thin = LB.Setup(sponge_t=3, pad=12, layer=0, **common)
+    thick = LB.Setup(sponge_t=20, pad=12, layer=0, **common)
+    net = semgb.Mlp(3)
+    t0 = time.perf_counter()
+    log = LB.train_network(thin, net, rounds=2, epochs=10, per_step=3000, seed=0)
+    t_train = time.perf_counter() - t0
+    e_net, _ = LB.reflected_energy(thin, net)
+    e_thin, _ = LB.reflected_energy(thin, None)
+    e_thick, _ = LB.reflected_energy(thick, None)
+    # speed at size
+    stream = torch.cuda.Stream()
+    out = {}
+    for name, ne, sponge, use_net in (("sponge20_120c", 120, 20, False), ("net_sponge3_86c", 86, 3, True)):
+        mesh = semgb.Mesh(ne, ne, ne, ne * h, ne * h, ne * h, o)
+        mesh.set_velocity(np.full(ne ** 3, c, np.float32))
+        sol = semgb.Solver(mesh, dt)
+        sol.set_kernel(semgb.KERNEL_STENCIL)
+        sol.set_stream(stream.cuda_stream)
+        sol.set_sponge(sponge, 0.06)
+        sol.set_source_points(np.array([[ne * h / 2] * 3], np.float32), semgb.ricker(200, dt, 10.0, 1)[None])
+        abc = semgb.Abc(sol, net, 0) if use_net else None
+        run = (lambda k: abc.step(k)) if use_net else (lambda k: sol.step(k))
+        run(4)
+        ms = _ev_time(stream, lambda: run(steps_time)) / steps_time
+        sol.synchronize()
+        out[name] = {"elements": ne, "nodes": mesh.n_nodes, "ms_per_step": ms,
+                     "boundary_nodes": abc.n_nodes if abc else 0}
+        if abc:
+            abc.close()
+        sol.close()
+        mesh.close()
+    net.close()
+    return {"quality": {"region": "6^3 Q4 elements", "reflected_energy_network_sponge3": e_net,
+                        "reflected_energy_sponge3": e_thin, "reflected_energy_sponge20": e_thick,
+                        "training": log, "training_seconds": t_train},
+            "speed": out,
+            "speedup_per_step": out["sponge20_120c"]["ms_per_step"] / out["net_sponge3_86c"]["ms_per_step"]}
 
 
 def main():

@@ -412,31 +412,34 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
     const int64_t plane = a.nxp * a.nz;
     for (int64_t row0 = (int64_t)blockIdx.x * T; row0 < a.n; row0 += (int64_t)gridDim.x * T) {
         __syncthreads();
-        // gather: feature (level l, neighbour (dz, dy, dx)) -> l*27 + (dz+1)*9 + (dy+1)*3 + (dx+1)
-        for (int i = threadIdx.x; i < T * kMlpIn; i += blockDim.x) {
-            const int r = i / kMlpIn, f = i - r * kMlpIn;
+        // gather, one thread per node: feature (level l, neighbour (dz, dy, dx)) ->
+        // l*27 + (dz+1)*9 + (dy+1)*3 + (dx+1); the node's coordinates are decoded once
+        {
+            const int r = threadIdx.x;  // 128 threads, one row each
             const int64_t row = row0 + r;
-            float v = 0.f;
+            float m = 0.f;
             if (row < a.n) {
-                const int l = f / 27, nb = f - l * 27;
-                const int dz = nb / 9 - 1, dy = (nb / 3) % 3 - 1, dx = nb % 3 - 1;
                 const int64_t q0 = a.nodes[row];
                 const int64_t iy = q0 / plane, rr = q0 - iy * plane, iz = rr / a.nxp, ix = rr - iz * a.nxp;
-                const int64_t jx = ix + dx, jy = iy + dy, jz = iz + dz;
-                if (jx >= 0 && jx < a.nx && jy >= 0 && jy < a.ny && jz >= 0 && jz < a.nz) {
-                    const int64_t qj = jx + jz * a.nxp + jy * plane;
-                    if (l == 0) v = a.p_new[qj];
-                    else if (l == 1) v = a.p_cur[qj] * (a.sx ? (a.sx[jx] * a.sy[jy]) * a.sz[jz] : 1.f);
-                    else v = a.hist[qj];
+                int f = 0;
+                for (int l = 0; l < 3; l++) {
+                    const float *lv = l == 0 ? a.p_new : (l == 1 ? a.p_cur : a.hist);
+                    for (int dz = -1; dz <= 1; dz++)
+                        for (int dy = -1; dy <= 1; dy++)
+                            for (int dx = -1; dx <= 1; dx++, f++) {
+                                const int64_t jx = ix + dx, jy = iy + dy, jz = iz + dz;
+                                float v = 0.f;
+                                if (jx >= 0 && jx < a.nx && jy >= 0 && jy < a.ny && jz >= 0 && jz < a.nz) {
+                                    v = lv[jx + jz * a.nxp + jy * plane];
+                                    if (l == 1 && a.sx) v *= (a.sx[jx] * a.sy[jy]) * a.sz[jz];
+                                }
+                                xf[r * kMlpIn + f] = v;
+                                m = fmaxf(m, fabsf(v));
+                            }
                 }
+            } else {
+                for (int f = 0; f < kMlpIn; f++) xf[r * kMlpIn + f] = 0.f;
             }
-            xf[r * kMlpIn + f] = v;
-        }
-        __syncthreads();
-        {
-            const int r = threadIdx.x;  // one row per thread (128 threads)
-            float m = 0.f;
-            for (int f = 0; f < kMlpIn; f++) m = fmaxf(m, fabsf(xf[r * kMlpIn + f]));
             scale[r] = m + 1e-30f;
         }
         __syncthreads();
@@ -560,9 +563,15 @@ cudaError_t abc_correction(const MlpDev &net, const AbcArgs &a, cudaStream_t s)
 {
     if (a.n <= 0) return cudaSuccess;
     const size_t sm = smem_abc();
-    cudaError_t e = cudaFuncSetAttribute(k_abc_correction, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    k_abc_correction<<<grid_for(a.n), T, sm, s>>>(net, a);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_abc_correction, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    // every tile its own CTA: the gather is latency-bound and wants many resident tiles
+    const int64_t tiles = (a.n + T - 1) / T;
+    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 1 << 20), T, sm, s>>>(net, a);
     return cudaGetLastError();
 }
 

@@ -11,9 +11,9 @@ network inputs of that step (sem_abc_features) with the target p_P^{n+1} / scale
 nodes (the face value of the padded run) or (p_P^{n+1} - p_T^{n+1}) / scale on interior strip
 nodes (the correction that would have reproduced the padded run).
 
-Evaluation: T runs from rest with and without the network; the reflected energy is
-sum over steps and interior nodes (the strip excluded) of (p_T - p_P)^2, divided by the same sum
-of p_P^2.
+Evaluation: T runs from rest with and without the network; the reflected energy is the sum over
+steps and the nodes of the region of interest of (p_T - p_P)^2, divided by the same sum of p_P^2.
+Set-ups with different sponges around the same region of interest compare directly.
 """
 from __future__ import annotations
 
@@ -27,19 +27,23 @@ from . import LEVEL_CURRENT, LEVEL_PREVIOUS, KERNEL_STENCIL, Abc, Mesh, Mlp, Sol
 
 @dataclass
 class Setup:
-    ex: int                  # elements per axis of the truncated mesh T
+    interior: int            # elements per axis of the region of interest
+    sponge_t: int            # sponge of T around it (elements): T has interior + 2 sponge_t elements
     order: int
     h: float
     c: float                 # velocity (m/s)
-    pad: int                 # extra elements per side of the padded mesh P
-    sponge_t: int            # sponge of T (elements)
+    pad: int                 # extra elements per side of the padded mesh P around T
     sponge_p: int            # sponge of P (elements)
     layer: int               # strip of the network (elements; 0: the boundary nodes)
     f0: float
     dt: float
     steps: int
-    src_frac: tuple = (0.5, 0.5, 0.5)  # source position as a fraction of T's box
+    src_frac: tuple = (0.5, 0.5, 0.5)  # source position as a fraction of the region of interest
     sigma: float = 0.06
+
+    @property
+    def ex(self):
+        return self.interior + 2 * self.sponge_t
 
     @property
     def nx_t(self):
@@ -51,6 +55,7 @@ class Setup:
 
 
 def _solver(s: Setup, ne: int, sponge: int, shift: float):
+    """Box of ne elements whose region of interest starts at `shift` metres."""
     L = ne * s.h
     mesh = Mesh(ne, ne, ne, L, L, L, s.order)
     mesh.set_velocity(np.full(ne ** 3, s.c, np.float32))
@@ -58,15 +63,16 @@ def _solver(s: Setup, ne: int, sponge: int, shift: float):
     sol.set_kernel(KERNEL_STENCIL)
     if sponge > 0:
         sol.set_sponge(sponge, s.sigma)
-    Lt = s.ex * s.h
-    xyz = np.array([[shift + f * Lt for f in s.src_frac]], np.float32)
+    Li = s.interior * s.h
+    xyz = np.array([[shift + f * Li for f in s.src_frac]], np.float32)
     sol.set_source_points(xyz, ricker(s.steps + 2, s.dt, s.f0, 1)[None])
     return mesh, sol
 
 
 def make_solvers(s: Setup):
     """(mesh_T, solver_T), (mesh_P, solver_P) with the source at the same physical point."""
-    return _solver(s, s.ex, s.sponge_t, 0.0), _solver(s, s.ex + 2 * s.pad, s.sponge_p, s.pad * s.h)
+    return (_solver(s, s.ex, s.sponge_t, s.sponge_t * s.h),
+            _solver(s, s.ex + 2 * s.pad, s.sponge_p, (s.pad + s.sponge_t) * s.h))
 
 
 def restrict(s: Setup, field_p):
@@ -175,11 +181,11 @@ def train_network(s: Setup, net: Mlp, rounds: int = 3, epochs: int = 12, per_ste
 
 
 def interior_mask(s: Setup):
-    """T's nodes outside the strip and the sponge (reference numbering)."""
+    """T's nodes in the region of interest (reference numbering)."""
     n = s.nx_t
-    w = max(s.layer, s.sponge_t, 1) * s.order
+    lo, hi = s.sponge_t * s.order, (s.sponge_t + s.interior) * s.order
     i = np.arange(n)
-    a = (i > w) & (i < n - 1 - w)
+    a = (i >= lo) & (i <= hi)
     return (a[:, None, None] & a[None, :, None] & a[None, None, :]).reshape(-1)
 
 

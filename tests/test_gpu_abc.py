@@ -116,8 +116,8 @@ def test_trained_network_reduces_reflections(semgb_lib, cuda_device):
     from semgb import workloads as W
     c, h, o = 2000.0, 10.0, 4
     dt = W.cfl_dt(h, o, c)
-    s = LB.Setup(ex=10, order=o, h=h, c=c, pad=10, sponge_t=2, sponge_p=6, layer=0, f0=40.0, dt=dt, steps=260,
-                 src_frac=(0.35, 0.5, 0.5))
+    s = LB.Setup(interior=6, sponge_t=2, order=o, h=h, c=c, pad=10, sponge_p=6, layer=0, f0=40.0, dt=dt,
+                 steps=260, src_frac=(0.25, 0.5, 0.5))
     net = semgb.Mlp(3)
     log = LB.train_network(s, net, rounds=2, epochs=10, per_step=3000, seed=0)
     print(log)
