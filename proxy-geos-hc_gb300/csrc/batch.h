@@ -10,7 +10,7 @@ namespace semgb {
 // Tuning knobs the autotuner picks (sem_batch_autotune).
 struct BatchTuning {
     int shots_per_lane = 1;  // one shot per lane: a warp covers 32 shots
-    int warps_per_cta = 4;   // element spans (neighbouring z-rows) per CTA: 2 or 4
+    int warps_per_cta = 8;   // z-rows of one element span per CTA (fixed at 8)
     int ychunk = 0;          // planes per CTA along y, rounded up to whole elements (0: all)
 };
 

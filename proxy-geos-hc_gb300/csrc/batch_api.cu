@@ -121,15 +121,15 @@ int prepare(sem_batch *b, int64_t n_new)
     return SEM_OK;
 }
 
-// Launch shapes the autotuner tries: 2 or 4 element spans per CTA, and whole columns or
-// y-chunks of about a quarter or an eighth of the planes (whole elements; the carried partial
-// sum costs one extra element of loads per chunk).
+// Launch shapes the autotuner tries: whole columns or y-chunks of about a half, a quarter or an
+// eighth of the planes (whole elements; the carried partial sum costs one extra element of
+// loads per chunk).  The CTA is fixed at 8 z-rows of one element span.
 std::vector<BatchTuning> candidates(const sem_batch *b)
 {
     std::vector<BatchTuning> v;
     const int64_t ny = b->mesh->box.ny, o = b->mesh->box.order;
-    for (int wpc : {2, 4})
-        for (int64_t div : {1, 4, 8}) {
+    for (int wpc : {8})
+        for (int64_t div : {1, 2, 4, 8}) {
             const int64_t chunk = ((ny + div - 1) / div + o - 1) / o * o;
             if (div > 1 && chunk < 8 * o) continue;
             BatchTuning t;
@@ -195,7 +195,7 @@ int sem_batch_create(sem_mesh *m, float dt, int n_shots, sem_batch **out)
         return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     if ((e = ensure_tables()) != cudaSuccess) return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     b->tune.shots_per_lane = 1;
-    b->tune.warps_per_cta = 4;
+    b->tune.warps_per_cta = 8;
     b->tune.ychunk = (int)std::max<int64_t>(8 * m->box.order, (m->box.ny / 8 + m->box.order - 1) / m->box.order * m->box.order);
     *out = b;
     return SEM_OK;

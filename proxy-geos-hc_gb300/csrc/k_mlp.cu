@@ -64,8 +64,20 @@ struct NetSmem {
 
 __device__ void load_net(NetSmem &s, const MlpDev &net)
 {
-    for (int i = threadIdx.x; i < H * kMlpInPad; i += blockDim.x) s.w1[(i / kMlpInPad) * KP1 + i % kMlpInPad] = net.w1[i];
-    for (int i = threadIdx.x; i < H * H; i += blockDim.x) s.w2[(i / H) * KP2 + i % H] = net.w2[i];
+    // 16-byte chunks: W1 rows are 96 bf16 (12 chunks), W2 rows 64 (8 chunks); shared rows are
+    // padded to 104 and 72 elements, still 16-byte aligned
+    constexpr int C1 = kMlpInPad / 8, C2 = H / 8;
+    static_assert((KP1 * 2) % 16 == 0 && (KP2 * 2) % 16 == 0, "16-byte aligned shared rows");
+#pragma unroll 4
+    for (int i = threadIdx.x; i < H * C1; i += blockDim.x) {
+        const int nn = i / C1, j = i - nn * C1;
+        *reinterpret_cast<uint4 *>(s.w1 + nn * KP1 + j * 8) = __ldg(reinterpret_cast<const uint4 *>(net.w1) + i);
+    }
+#pragma unroll 4
+    for (int i = threadIdx.x; i < H * C2; i += blockDim.x) {
+        const int nn = i / C2, j = i - nn * C2;
+        *reinterpret_cast<uint4 *>(s.w2 + nn * KP2 + j * 8) = __ldg(reinterpret_cast<const uint4 *>(net.w2) + i);
+    }
     for (int i = threadIdx.x; i < H; i += blockDim.x) {
         s.b1[i] = net.b1[i];
         s.b2[i] = net.b2[i];
@@ -413,7 +425,8 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
     for (int64_t row0 = (int64_t)blockIdx.x * T; row0 < a.n; row0 += (int64_t)gridDim.x * T) {
         __syncthreads();
         // gather, one thread per node: feature (level l, neighbour (dz, dy, dx)) ->
-        // l*27 + (dz+1)*9 + (dy+1)*3 + (dx+1); the node's coordinates are decoded once
+        // l*27 + (dz+1)*9 + (dy+1)*3 + (dx+1); coordinates decoded once, the 27 loads of a level
+        // unrolled so that they are in flight together, sponge factors as 3+3+3 axis values
         {
             const int r = threadIdx.x;  // 128 threads, one row each
             const int64_t row = row0 + r;
@@ -421,21 +434,35 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
             if (row < a.n) {
                 const int64_t q0 = a.nodes[row];
                 const int64_t iy = q0 / plane, rr = q0 - iy * plane, iz = rr / a.nxp, ix = rr - iz * a.nxp;
-                int f = 0;
+                bool okx[3], oky[3], okz[3];
+                float fx[3], fy[3], fz[3];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    okx[d] = ix + d - 1 >= 0 && ix + d - 1 < a.nx;
+                    oky[d] = iy + d - 1 >= 0 && iy + d - 1 < a.ny;
+                    okz[d] = iz + d - 1 >= 0 && iz + d - 1 < a.nz;
+                    fx[d] = (a.sx && okx[d]) ? __ldg(a.sx + ix + d - 1) : 1.f;
+                    fy[d] = (a.sx && oky[d]) ? __ldg(a.sy + iy + d - 1) : 1.f;
+                    fz[d] = (a.sx && okz[d]) ? __ldg(a.sz + iz + d - 1) : 1.f;
+                }
+#pragma unroll 1
                 for (int l = 0; l < 3; l++) {
                     const float *lv = l == 0 ? a.p_new : (l == 1 ? a.p_cur : a.hist);
-                    for (int dz = -1; dz <= 1; dz++)
-                        for (int dy = -1; dy <= 1; dy++)
-                            for (int dx = -1; dx <= 1; dx++, f++) {
-                                const int64_t jx = ix + dx, jy = iy + dy, jz = iz + dz;
-                                float v = 0.f;
-                                if (jx >= 0 && jx < a.nx && jy >= 0 && jy < a.ny && jz >= 0 && jz < a.nz) {
-                                    v = lv[jx + jz * a.nxp + jy * plane];
-                                    if (l == 1 && a.sx) v *= (a.sx[jx] * a.sy[jy]) * a.sz[jz];
-                                }
-                                xf[r * kMlpIn + f] = v;
-                                m = fmaxf(m, fabsf(v));
-                            }
+                    float v[27];
+#pragma unroll
+                    for (int nb = 0; nb < 27; nb++) {
+                        const int dz = nb / 9, dy = (nb / 3) % 3, dx = nb % 3;
+                        v[nb] = (okx[dx] && oky[dy] && okz[dz])
+                                    ? lv[(ix + dx - 1) + (iz + dz - 1) * a.nxp + (iy + dy - 1) * plane]
+                                    : 0.f;
+                    }
+#pragma unroll
+                    for (int nb = 0; nb < 27; nb++) {
+                        const int dz = nb / 9, dy = (nb / 3) % 3, dx = nb % 3;
+                        const float w = l == 1 ? v[nb] * ((fx[dx] * fy[dy]) * fz[dz]) : v[nb];
+                        xf[r * kMlpIn + l * 27 + nb] = w;
+                        m = fmaxf(m, fabsf(w));
+                    }
                 }
             } else {
                 for (int f = 0; f < kMlpIn; f++) xf[r * kMlpIn + f] = 0.f;
@@ -443,9 +470,15 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
             scale[r] = m + 1e-30f;
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < T * kMlpInPad; i += blockDim.x) {
-            const int r = i / kMlpInPad, k = i - r * kMlpInPad;
-            xs[r * KP1 + k] = f2bf(k < kMlpIn ? xf[r * kMlpIn + k] / scale[r] : 0.f);
+        {
+            const int r = threadIdx.x;
+            const float inv = 1.f / scale[r];
+#pragma unroll 8
+            for (int k = 0; k < kMlpInPad; k += 2) {
+                const float u0 = k < kMlpIn ? xf[r * kMlpIn + k] * inv : 0.f;
+                const float u1 = k + 1 < kMlpIn ? xf[r * kMlpIn + k + 1] * inv : 0.f;
+                *reinterpret_cast<uint32_t *>(xs + r * KP1 + k) = pack_bf2(u0, u1);
+            }
         }
         __syncthreads();
         float yv[2][2];
@@ -569,9 +602,9 @@ cudaError_t abc_correction(const MlpDev &net, const AbcArgs &a, cudaStream_t s)
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    // every tile its own CTA: the gather is latency-bound and wants many resident tiles
+    // persistent CTAs (two per SM fit the shared memory): the weights are staged once per CTA
     const int64_t tiles = (a.n + T - 1) / T;
-    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 1 << 20), T, sm, s>>>(net, a);
+    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 152 * 2), T, sm, s>>>(net, a);
     return cudaGetLastError();
 }
 
