@@ -551,6 +551,41 @@ def measure_learned(steps_time: int = 40):
             "speedup_per_step": out["sponge20_120c"]["ms_per_step"] / out["net_sponge3_86c"]["ms_per_step"]}
 
 
+def run_case(name: str):
+    """Small fixed cases for kernel profiles (no JSON line): `batch40` steps a 64-shot batch on a
+    40^3 Q4 mesh 6 times; `abc86` runs 6 steps of an 86^3 Q4 mesh with the boundary network."""
+    import semgb
+    from semgb import workloads as W
+    if name == "batch40":
+        wl = W.c3_batched_shots(40, 64, 50)
+        mesh = semgb.Mesh(wl.ex, wl.ey, wl.ez, wl.lx, wl.ly, wl.lz, wl.order)
+        mesh.set_velocity(wl.vel)
+        wav = np.stack([semgb.ricker(wl.nsteps, wl.dt, float(f), 1) for f in wl.f0])
+        b = semgb.Batch(mesh, wl.dt, 64)
+        b.set_sponge(wl.sponge_thickness, wl.sponge_sigma)
+        b.set_source_points(wl.src_xyz, wav)
+        b.set_receivers(wl.rec_xyz)
+        b.step(6)
+        b.synchronize()
+        print("batch40 ok", mesh.n_nodes)
+    elif name == "abc86":
+        ne, o, h, c = 86, 4, 10.0, 2000.0
+        dt = W.cfl_dt(h, o, c)
+        mesh = semgb.Mesh(ne, ne, ne, ne * h, ne * h, ne * h, o)
+        mesh.set_velocity(np.full(ne ** 3, c, np.float32))
+        sol = semgb.Solver(mesh, dt)
+        sol.set_kernel(semgb.KERNEL_STENCIL)
+        sol.set_sponge(3, 0.06)
+        sol.set_source_points(np.array([[ne * h / 2] * 3], np.float32), semgb.ricker(200, dt, 10.0, 1)[None])
+        net = semgb.Mlp(3)
+        abc = semgb.Abc(sol, net, 0)
+        abc.step(6)
+        sol.synchronize()
+        print("abc86 ok", abc.n_nodes)
+    else:
+        raise SystemExit(f"unknown case {name}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -565,7 +600,12 @@ def main():
     ap.add_argument("--ref-elems", type=int, default=32, help="--impl reference sub-box (elements per axis)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-rows", action="store_true", help="skip the batched / uneven / adjoint rows")
+    ap.add_argument("--case", choices=["batch40", "abc86"], default=None,
+                    help="run a small fixed case for a kernel profile instead of the benchmark")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
