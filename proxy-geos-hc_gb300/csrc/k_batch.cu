@@ -328,21 +328,6 @@ __global__ void k_batch_record(const BatchRecordArgs a)
     a.traces[((int64_t)step * a.nrec + r) * a.nshot + s] = a.level[a.rec_node[r] * a.s_pad + s];
 }
 
-template <int O>
-cudaError_t launch_o(const BatchArgs &a0, bool sponge, int wpc, cudaStream_t st)
-{
-    BatchArgs a = a0;
-    a.ychunk = (a.ychunk + O - 1) / O * O;
-    if (a.s_pad % 32) return cudaErrorInvalidValue;
-    const int ex = (int)((a.nx - 1) / O);
-    const int64_t warps = (int64_t)ex * a.nz;
-    const dim3 grid((unsigned)((warps + wpc - 1) / wpc), (unsigned)((a.ny + a.ychunk - 1) / a.ychunk),
-                    (unsigned)(a.s_pad / 32));
-    if (sponge) k_batch<O, true><<<grid, 32 * wpc, 0, st>>>(a, ex);
-    else k_batch<O, false><<<grid, 32 * wpc, 0, st>>>(a, ex);
-    return cudaGetLastError();
-}
-
 }  // namespace
 
 cudaError_t batch_kernel_setup(const float *T_all, const float *wa_all)
