@@ -105,8 +105,20 @@ __device__ __forceinline__ VecO<O> axis_uniform(const float (&c)[O], const RowFn
         float v[O];
         load_o<O>(row(d), v);
         const float t = c_T[O - 1][LOC * (2 * O + 1) + d + O];
+        if constexpr (O % 2 == 0) {
+            // the coefficient is shared by the thread's nodes: pairs of nodes in packed f32x2
+            // (each half rounds as the scalar sub and fma would)
 #pragma unroll
-        for (int j = 0; j < O; j++) r.v[j] = fmaf(t, v[j] - c[j], r.v[j]);
+            for (int j = 0; j < O; j += 2) {
+                const float2 acc = fma2(make_float2(t, t), sub2(make_float2(v[j], v[j + 1]), make_float2(c[j], c[j + 1])),
+                                        make_float2(r.v[j], r.v[j + 1]));
+                r.v[j] = acc.x;
+                r.v[j + 1] = acc.y;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < O; j++) r.v[j] = fmaf(t, v[j] - c[j], r.v[j]);
+        }
     }
     return r;
 }
