@@ -7,14 +7,15 @@
 // form sum_d T[l][d] (p_{i+d} - p_i), exactly zero for a constant field.
 //
 // Work decomposition (HBM-bound pass: read p^n, p^{n-1}, dt^2/M, write p^{n+1}; 16 B/node):
-//  - a CTA owns a tile of TX = 32*o nodes along x by TZ rows along z and marches along y over a
-//    chunk of planes; warp = row, lane = one element's o consecutive x-nodes, so a node's local x
-//    index is a compile-time constant (x-coefficients are immediates, zero terms are skipped);
-//    the z- and y-local indices are warp-uniform and select specialised code;
+//  - a CTA owns a tile of TX nodes along x by TZ rows along z and marches along y over a chunk
+//    of planes; a lane holds one element's o consecutive x-nodes, so a node's local x index is a
+//    compile-time constant (x-coefficients are immediates, zero terms are skipped); a warp covers
+//    RW rows o apart (RW = 2 for o = 1, 2, 4: 16 lanes per row, TX = 16*o), so the z- and
+//    y-local indices are warp-uniform and select specialised code;
 //  - one elected thread streams y-planes into shared memory with 3-D TMA tile loads completed on
-//    mbarriers: a ring of 2o+1+L planes of p^n (tile rows with an x halo) serves the x- and
-//    y-neighbours, and per-plane "aux" slots hold the z-halo rows of p^n plus the p^{n-1} and
-//    dt^2/M tiles; loads run L planes ahead of the compute;
+//    mbarriers: a ring of 2o+1+L planes of p^n (tile rows plus the z halo, with an x halo) serves
+//    the x-, y- and z-neighbours, and per-plane "aux" slots hold the p^{n-1} and dt^2/M tiles;
+//    loads run L planes ahead of the compute;
 //  - one barrier per plane; every mbarrier wait is bounded (tma.cuh) and a timeout is reported
 //    through a status word instead of hanging.
 #include <cuda.h>
@@ -35,7 +36,10 @@ namespace {
 #define SEM_STENCIL_LOOKAHEAD 1
 #endif
 #ifndef SEM_STENCIL_ROWS
-#define SEM_STENCIL_ROWS 8
+#define SEM_STENCIL_ROWS 8  // warps per CTA
+#endif
+#ifndef SEM_STENCIL_RW
+#define SEM_STENCIL_RW 2  // rows per warp where the order allows it
 #endif
 constexpr int kLook = SEM_STENCIL_LOOKAHEAD;  // planes of lookahead
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
@@ -45,9 +49,15 @@ __constant__ float c_wa[kMaxOrder][kMaxOrder];  // assembled weights by local in
 
 template <int O>
 struct Cfg {
-    static constexpr int TZ = O == 5 ? 8 : SEM_STENCIL_ROWS;  // rows (warps) per CTA
-    static constexpr int THREADS = 32 * TZ;
-    static constexpr int TX = 32 * O;                   // nodes along x per CTA
+    static constexpr int WARPS = O == 5 ? 8 : SEM_STENCIL_ROWS;
+    // A warp's lanes split into RW groups on rows O apart, so that the z-local index stays
+    // warp-uniform (needs WARPS a multiple of O); narrower tiles waste fewer lanes on the last
+    // x-tile of a row (801 nodes: 13 tiles of 64 against 7 of 128).
+    static constexpr int RW = WARPS % O == 0 ? SEM_STENCIL_RW : 1;
+    static constexpr int LANES = 32 / RW;               // lanes per row
+    static constexpr int TZ = WARPS * RW;               // rows per CTA
+    static constexpr int THREADS = 32 * WARPS;
+    static constexpr int TX = LANES * O;                // nodes along x per CTA
     static constexpr int HX = O <= 4 ? 4 : 8;           // x halo, a multiple of 4 floats
     static constexpr int TXP = TX + 2 * HX;             // ring row length
     static constexpr int TZP = TZ + 2 * O;              // ring rows: tile plus z halo
@@ -82,6 +92,19 @@ __device__ __forceinline__ void load_o(const float *p, float (&v)[O])
     } else {
 #pragma unroll
         for (int j = 0; j < O; j++) v[j] = p[j];
+    }
+}
+
+// As load_o, for a run of which only the first `lim` values lie inside the row's allocation
+// (padding columns included); the others read as zero.
+template <int O>
+__device__ __forceinline__ void load_o_lim(const float *p, float (&v)[O], int lim)
+{
+    if (lim >= O) {
+        load_o<O>(p, v);
+    } else {
+#pragma unroll
+        for (int j = 0; j < O; j++) v[j] = j < lim ? p[j] : 0.f;
     }
 }
 
@@ -157,7 +180,7 @@ struct YPlanes {
 };
 
 template <int O, bool SPONGE, int MODE>
-__global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::TZ <= 8 ? 2 : 1)
+__global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::WARPS <= 8 ? 2 : 1)
     k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap prev_map,
               const __grid_constant__ CUtensorMap a_map, const StencilTables t, const StencilArgs a)
 {
@@ -202,18 +225,21 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::TZ <= 8 ? 2 : 1)
     }
 
     // per-thread constants
-    const int z = z0 + w;
+    // tile row and x group of the thread: rows of one warp share z mod O
+    const int xl = l % C::LANES;
+    const int rw = C::RW == 1 ? w : (w / O) * (O * C::RW) + w % O + (l / C::LANES) * O;
+    const int z = z0 + rw;
     const bool row_ok = z < nz;
     const bool zin = z > 0 && z < nz - 1;
     const int lz = z % O;
-    const int xb = x0 + O * l;  // first node of the thread
+    const int xb = x0 + O * xl;  // first node of the thread
     float sxv[O];
 #pragma unroll
     for (int j = 0; j < O; j++) sxv[j] = (SPONGE && xb + j < nx) ? __ldg(a.sx + xb + j) : 1.f;
     const float szv = (SPONGE && row_ok) ? __ldg(a.sz + z) : 1.f;
     const float wz = c_wa[O - 1][lz];
-    const int off = (w + O) * TXP + HX + O * l;  // in-slot offset of the thread's first node
-    const int toff = w * TX + O * l;             // in-tile offset (aux tiles)
+    const int off = (rw + O) * TXP + HX + O * xl;  // in-slot offset of the thread's first node
+    const int toff = rw * TX + O * xl;             // in-tile offset (aux tiles)
     float *dst_col = a.prev + (int64_t)xb + (int64_t)z * t.nxp;
     const int64_t plane_stride = t.nxp * t.nz;
 
@@ -273,7 +299,8 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::TZ <= 8 ? 2 : 1)
             const float syv = SPONGE ? __ldg(a.sy + y) : 1.f;
             const float gx = t.g[0] * (wz * wy), gzy = t.g[1] * wy, gyz = t.g[2] * wz;
             float out[O], kp[O];
-            if (MODE == STENCIL_GRADIENT) load_o<O>(a.kp + (dst_col - a.prev) + (int64_t)y * plane_stride, kp);
+            if (MODE == STENCIL_GRADIENT)
+                load_o_lim<O>(a.kp + (dst_col - a.prev) + (int64_t)y * plane_stride, kp, (int)t.nxp - xb);
 #pragma unroll
             for (int j = 0; j < O; j++) {
                 const float wxj = c_wa[O - 1][j];
@@ -294,7 +321,7 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::TZ <= 8 ? 2 : 1)
                 const int64_t off = dst - a.prev;
                 if (MODE == STENCIL_GRADIENT) {
                     float g[O];
-                    load_o<O>(a.grad + off, g);
+                    load_o_lim<O>(a.grad + off, g, (int)t.nxp - xb);
 #pragma unroll
                     for (int j = 0; j < O; j++) kp[j] = fmaf(c[j], kp[j], g[j]);
                 }
@@ -357,16 +384,19 @@ size_t smem_bytes(int order)
 }
 
 template <int O>
-void tile_of(int &tx, int &tz, int &hx) { tx = Cfg<O>::TX; tz = Cfg<O>::TZ; hx = Cfg<O>::HX; }
+void tile_of(int &tx, int &tz, int &hx, int &th)
+{
+    tx = Cfg<O>::TX; tz = Cfg<O>::TZ; hx = Cfg<O>::HX; th = Cfg<O>::THREADS;
+}
 
-void tile_dims(int order, int &tx, int &tz, int &hx)
+void tile_dims(int order, int &tx, int &tz, int &hx, int &th)
 {
     switch (order) {
-    case 1: tile_of<1>(tx, tz, hx); break;
-    case 2: tile_of<2>(tx, tz, hx); break;
-    case 3: tile_of<3>(tx, tz, hx); break;
-    case 4: tile_of<4>(tx, tz, hx); break;
-    default: tile_of<5>(tx, tz, hx); break;
+    case 1: tile_of<1>(tx, tz, hx, th); break;
+    case 2: tile_of<2>(tx, tz, hx, th); break;
+    case 3: tile_of<3>(tx, tz, hx, th); break;
+    case 4: tile_of<4>(tx, tz, hx, th); break;
+    default: tile_of<5>(tx, tz, hx, th); break;
     }
 }
 
@@ -453,7 +483,8 @@ int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, Stenc
     t->nx = b.nx; t->nxp = b.nxp; t->ny = b.ny; t->nz = b.nz;
     for (int d = 0; d < 3; d++) t->g[d] = (float)geo.g[d];
     for (int l = 0; l < b.order; l++) t->wa[l] = (float)(l == 0 ? g.w[0] + g.w[b.order] : g.w[l]);
-    tile_dims(b.order, t->tile_x, t->tile_z, t->halo_x);
+    int threads = 256;
+    tile_dims(b.order, t->tile_x, t->tile_z, t->halo_x, threads);
     t->smem = smem_bytes(b.order);
     t->grid[0] = (int)((b.nx + t->tile_x - 1) / t->tile_x);
     t->grid[1] = (int)((b.nz + t->tile_z - 1) / t->tile_z);
@@ -463,7 +494,7 @@ int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, Stenc
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    per_sm = std::max(1, std::min(2048 / (32 * t->tile_z), smem_sm / (int)(t->smem + 1024)));
+    per_sm = std::max(1, std::min(2048 / threads, smem_sm / (int)(t->smem + 1024)));
     const int64_t cols = (int64_t)t->grid[0] * t->grid[1];
     const int64_t resident = (int64_t)sms * per_sm;
     double best = 1e300;
