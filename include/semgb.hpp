@@ -93,6 +93,7 @@ public:
 
     sem_solver *handle() const { return h_; }
     void setKernel(int k) { check(sem_solver_set_kernel(h_, k), "sem_solver_set_kernel"); }
+    void setOperatorForm(int f) { check(sem_solver_set_operator_form(h_, f), "sem_solver_set_operator_form"); }
     void setSponge(int thickness, float sigma) { check(sem_solver_set_sponge(h_, thickness, sigma), "sem_solver_set_sponge"); }
     void setSources(const std::vector<int64_t> &elements, const std::vector<float> &wavelet, int nsamples)
     {

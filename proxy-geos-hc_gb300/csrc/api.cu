@@ -376,6 +376,18 @@ int sem_solver_set_kernel(sem_solver *s, int kernel)
     return SEM_OK;
 }
 
+int sem_solver_set_operator_form(sem_solver *s, int form)
+{
+    if (!s) return fail(SEM_ERR_ARG, "NULL solver");
+    if (form != SEM_FORM_DIRECT && form != SEM_FORM_DIFFERENCE) return fail(SEM_ERR_ARG, "unknown operator form");
+    if (form != s->form) {
+        cudaStreamSynchronize(s->stream);
+        solver_invalidate_graphs(s);
+        s->form = form;
+    }
+    return SEM_OK;
+}
+
 int sem_solver_set_sponge_profile(sem_solver *s, const float *sx, const float *sy, const float *sz)
 {
     GUARD_BEGIN
@@ -622,7 +634,8 @@ cudaError_t solver_enqueue_step(sem_solver *s, int c, cudaEvent_t *ev, const Ste
             ta.kp = extra->kp;
             ta.grad = extra->grad;
         }
-        if ((e = launch_stencil(*s->stencil, ta, c, s->sponge, s->stream, mode)) != cudaSuccess) return e;
+        const bool direct = s->form == SEM_FORM_DIRECT;
+        if ((e = launch_stencil(*s->stencil, ta, c, s->sponge, s->stream, mode, direct)) != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[2], s->stream);
     }
     if (ev) cudaEventRecord(ev[3], s->stream);

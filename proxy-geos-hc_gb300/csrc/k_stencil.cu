@@ -13,9 +13,10 @@
 //    RW rows o apart (RW = 2 for o = 1, 2, 4: 16 lanes per row, TX = 16*o), so the z- and
 //    y-local indices are warp-uniform and select specialised code;
 //  - one elected thread streams y-planes into shared memory with 3-D TMA tile loads completed on
-//    mbarriers: a ring of 2o+1+L planes of p^n (tile rows plus the z halo, with an x halo) serves
-//    the x-, y- and z-neighbours, and per-plane "aux" slots hold the p^{n-1} and dt^2/M tiles;
-//    loads run L planes ahead of the compute;
+//    mbarriers: a ring of 2o+1+L planes of p^n (tile rows only) serves the y-neighbours, and
+//    per-plane "aux" slots hold the p^{n-1} and dt^2/M tiles plus a window of the plane's p^n with
+//    its z and x halos (the x- and z-neighbours and the node itself); keeping the halos out of
+//    the ring halves its size, so three CTAs fit on an SM for o <= 4; loads run L planes ahead;
 //  - one barrier per plane; every mbarrier wait is bounded (tma.cuh) and a timeout is reported
 //    through a status word instead of hanging.
 #include <cuda.h>
@@ -59,20 +60,23 @@ struct Cfg {
     static constexpr int THREADS = 32 * WARPS;
     static constexpr int TX = LANES * O;                // nodes along x per CTA
     static constexpr int HX = O <= 4 ? 4 : 8;           // x halo, a multiple of 4 floats
-    static constexpr int TXP = TX + 2 * HX;             // ring row length
-    static constexpr int TZP = TZ + 2 * O;              // ring rows: tile plus z halo
+    static constexpr int TXP = TX + 2 * HX;             // window row length
+    static constexpr int TZP = TZ + 2 * O;              // window rows: tile plus z halo
     static constexpr int W = 2 * O + 1;
     static constexpr int R = W + kLook;                 // ring slots
     static constexpr int AUX = kLook + 1;               // aux slots
     static constexpr size_t al(size_t b) { return (b + 127) / 128 * 128; }
-    static constexpr int RING_FLOATS = (int)(al(sizeof(float) * TZP * TXP) / 4);
     static constexpr int TILE_FLOATS = (int)(al(sizeof(float) * TZ * TX) / 4);
-    static constexpr int AUX_FLOATS = 2 * TILE_FLOATS;  // p^{n-1} tile, dt^2/M tile
+    static constexpr int WIN_FLOATS = (int)(al(sizeof(float) * TZP * TXP) / 4);  // plane with halos
+    static constexpr int RING_FLOATS = TILE_FLOATS;     // y-ring: tile rows only
+    static constexpr int AUX_FLOATS = 2 * TILE_FLOATS + WIN_FLOATS;  // p^{n-1}, dt^2/M tiles; p^n window
     static constexpr size_t OFF_AUX = (size_t)R * RING_FLOATS * 4;
     static constexpr size_t OFF_BAR = OFF_AUX + (size_t)AUX * AUX_FLOATS * 4;
     static constexpr size_t SMEM = OFF_BAR + 8 * (R + AUX);
-    static constexpr uint32_t RING_TX = sizeof(float) * TZP * TXP;
-    static constexpr uint32_t AUX_TX = sizeof(float) * 2 * TZ * TX;
+    static constexpr uint32_t RING_TX = sizeof(float) * TZ * TX;
+    static constexpr uint32_t AUX_TX = sizeof(float) * (2 * TZ * TX + TZP * TXP);
+    // three CTAs per SM where shared memory allows (the register cap follows: 85 per thread)
+    static constexpr int MIN_BLOCKS = WARPS > 8 ? 1 : (SMEM <= 74 * 1024 ? 3 : 2);
 };
 
 // Offsets d with a non-zero coefficient for local index l: [-o, o] for l == 0 (element face),
@@ -116,10 +120,25 @@ struct VecO {
 // Axis term along a direction whose local index LOC is uniform over the thread's O nodes:
 // r[j] = sum_d T[LOC][d] (row(d)[j] - c[j]).  row(d) returns the pointer to the O values at
 // offset d along the axis.
-template <int O, int LOC, class RowFn>
+template <int O, int LOC, bool DIRECT, class RowFn>
 __device__ __forceinline__ VecO<O> axis_uniform(const float (&c)[O], const RowFn &row)
 {
     VecO<O> r;
+    if constexpr (DIRECT) {
+        // direct form: diagonal T[LOC][o] times the node, then one fma per neighbour; the
+        // coefficients are constant-bank operands of scalar fmas
+#pragma unroll
+        for (int j = 0; j < O; j++) r.v[j] = c_T[O - 1][LOC * (2 * O + 1) + O] * c[j];
+#pragma unroll
+        for (int d = dlo(O, LOC); d <= dhi(O, LOC); d++) {
+            if (d == 0) continue;
+            float v[O];
+            load_o<O>(row(d), v);
+#pragma unroll
+            for (int j = 0; j < O; j++) r.v[j] = fmaf(c_T[O - 1][LOC * (2 * O + 1) + d + O], v[j], r.v[j]);
+        }
+        return r;
+    }
 #pragma unroll
     for (int j = 0; j < O; j++) r.v[j] = 0.f;
 #pragma unroll
@@ -146,20 +165,20 @@ __device__ __forceinline__ VecO<O> axis_uniform(const float (&c)[O], const RowFn
     return r;
 }
 
-template <int O, class RowFn>
+template <int O, bool DIRECT, class RowFn>
 __device__ __forceinline__ VecO<O> axis_dispatch(int loc, const float (&c)[O], const RowFn &row)
 {
     switch (loc) {
-    case 0: return axis_uniform<O, 0>(c, row);
-    case 1: if constexpr (O > 1) return axis_uniform<O, 1>(c, row);
-    case 2: if constexpr (O > 2) return axis_uniform<O, 2>(c, row);
-    case 3: if constexpr (O > 3) return axis_uniform<O, 3>(c, row);
-    default: if constexpr (O > 4) return axis_uniform<O, 4>(c, row);
+    case 0: return axis_uniform<O, 0, DIRECT>(c, row);
+    case 1: if constexpr (O > 1) return axis_uniform<O, 1, DIRECT>(c, row);
+    case 2: if constexpr (O > 2) return axis_uniform<O, 2, DIRECT>(c, row);
+    case 3: if constexpr (O > 3) return axis_uniform<O, 3, DIRECT>(c, row);
+    default: if constexpr (O > 4) return axis_uniform<O, 4, DIRECT>(c, row);
     }
-    return axis_uniform<O, 0>(c, row);  // not reached: loc < O
+    return axis_uniform<O, 0, DIRECT>(c, row);  // not reached: loc < O
 }
 
-// z-neighbour rows: ring slot rows are contiguous over the tile and its z halo.
+// z-neighbour rows: window rows are contiguous over the tile and its z halo.
 struct ZRows {
     const float *base;  // current plane, row of the thread's node, first column of its nodes
     int txp;
@@ -179,10 +198,11 @@ struct YPlanes {
     }
 };
 
-template <int O, bool SPONGE, int MODE>
-__global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::WARPS <= 8 ? 2 : 1)
-    k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap prev_map,
-              const __grid_constant__ CUtensorMap a_map, const StencilTables t, const StencilArgs a)
+template <int O, bool SPONGE, int MODE, bool DIRECT>
+__global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
+    k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap win_map,
+              const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap a_map,
+              const StencilTables t, const StencilArgs a)
 {
     using C = Cfg<O>;
     constexpr int TZ = C::TZ, TX = C::TX, HX = C::HX, TXP = C::TXP, R = C::R, AUX = C::AUX;
@@ -199,11 +219,11 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::WARPS <= 8 ? 2 : 1)
     const int nx = (int)t.nx, nz = (int)t.nz, ny = (int)t.ny;
 
     // ring plane p (p >= yb - O) lives in slot (p - yb + O) % R; aux plane p in (p - yb) % AUX
-    const CUtensorMap *rmap = &ring_map, *pmap = &prev_map, *amap = &a_map;  // parameter space
+    const CUtensorMap *rmap = &ring_map, *wmap = &win_map, *pmap = &prev_map, *amap = &a_map;  // parameter space
     auto issue_ring = [=](int p) {
         const int i = (p - yb + O) % R;
         bar_arrive_expect_tx(bars + i, C::RING_TX);
-        tma_load_3d(ring + i * C::RING_FLOATS, rmap, x0 - HX, z0 - O, p, bars + i);
+        tma_load_3d(ring + i * C::RING_FLOATS, rmap, x0, z0, p, bars + i);
     };
     auto issue_aux = [=](int p) {
         const int i = (p - yb) % AUX;
@@ -211,6 +231,7 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::WARPS <= 8 ? 2 : 1)
         bar_arrive_expect_tx(bars + R + i, C::AUX_TX);
         tma_load_3d(b, pmap, x0, z0, p, bars + R + i);
         tma_load_3d(b + C::TILE_FLOATS, amap, x0, z0, p, bars + R + i);
+        tma_load_3d(b + 2 * C::TILE_FLOATS, wmap, x0 - HX, z0 - O, p, bars + R + i);
     };
 
     if (threadIdx.x == 0) {
@@ -238,8 +259,8 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::WARPS <= 8 ? 2 : 1)
     for (int j = 0; j < O; j++) sxv[j] = (SPONGE && xb + j < nx) ? __ldg(a.sx + xb + j) : 1.f;
     const float szv = (SPONGE && row_ok) ? __ldg(a.sz + z) : 1.f;
     const float wz = c_wa[O - 1][lz];
-    const int off = (rw + O) * TXP + HX + O * xl;  // in-slot offset of the thread's first node
-    const int toff = rw * TX + O * xl;             // in-tile offset (aux tiles)
+    const int off = (rw + O) * TXP + HX + O * xl;  // offset of the thread's first node in the window
+    const int toff = rw * TX + O * xl;             // in-tile offset (aux tiles, y-ring slots)
     float *dst_col = a.prev + (int64_t)xb + (int64_t)z * t.nxp;
     const int64_t plane_stride = t.nxp * t.nz;
 
@@ -266,7 +287,7 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::WARPS <= 8 ? 2 : 1)
             if (!ok) { s_abort = 1; atomicExch(a.status, 1); }
         }
         if (row_ok) {
-            const float *cur = ring + rs * C::RING_FLOATS + off;
+            const float *cur = aux + as * C::AUX_FLOATS + 2 * C::TILE_FLOATS + off;  // window
             const float *tq = aux + as * C::AUX_FLOATS + toff;
             float c[O], left[O], q[O], am[O];
             load_o<O>(cur, c);
@@ -279,7 +300,7 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::WARPS <= 8 ? 2 : 1)
             float ax[O];
 #pragma unroll
             for (int j = 0; j < O; j++) {
-                float acc = 0.f;
+                float acc = DIRECT ? c_T[O - 1][j * (2 * O + 1) + O] * c[j] : 0.f;
                 // constant trip count, so that the loop unrolls together with j and every index
                 // below is a constant (a j-dependent range left it rolled, with the arrays in memory)
 #pragma unroll
@@ -287,12 +308,12 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::WARPS <= 8 ? 2 : 1)
                     if (d == 0 || d < dlo(O, j) || d > dhi(O, j)) continue;
                     const int m = j + d;  // offset from the thread's first node, in [-O, O]
                     const float v = m < 0 ? left[m + O] : (m < O ? c[m] : right);
-                    acc = fmaf(c_T[O - 1][j * (2 * O + 1) + d + O], v - c[j], acc);
+                    acc = fmaf(c_T[O - 1][j * (2 * O + 1) + d + O], DIRECT ? v : v - c[j], acc);
                 }
                 ax[j] = acc;
             }
-            const VecO<O> az = axis_dispatch<O>(lz, c, ZRows{cur, TXP});
-            const VecO<O> ay = axis_dispatch<O>(ly, c, YPlanes{ring, rs, R, C::RING_FLOATS, off});
+            const VecO<O> az = axis_dispatch<O, DIRECT>(lz, c, ZRows{cur, TXP});
+            const VecO<O> ay = axis_dispatch<O, DIRECT>(ly, c, YPlanes{ring, rs, R, C::RING_FLOATS, toff});
 
             const bool yin = y > 0 && y < ny - 1;
             const float wy = c_wa[O - 1][ly];
@@ -400,47 +421,86 @@ void tile_dims(int order, int &tx, int &tz, int &hx, int &th)
     }
 }
 
-template <int O, bool SPONGE, int MODE>
+// resident CTAs per SM of the sponge variant (the others use no more registers); 0 if unknown
+template <int O>
+int blocks_per_sm_of()
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stencil<O, true, STENCIL_PLAIN, true>, Cfg<O>::THREADS,
+                                                      Cfg<O>::SMEM) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    return n;
+}
+
+int blocks_per_sm(int order)
+{
+    switch (order) {
+    case 1: return blocks_per_sm_of<1>();
+    case 2: return blocks_per_sm_of<2>();
+    case 3: return blocks_per_sm_of<3>();
+    case 4: return blocks_per_sm_of<4>();
+    default: return blocks_per_sm_of<5>();
+    }
+}
+
+template <int O, bool SPONGE, int MODE, bool DIRECT>
 void launch_om(const dim3 &grid, const LevelMaps &cm, const LevelMaps &pm, const StencilTables &t,
                const StencilArgs &a, cudaStream_t s)
 {
-    k_stencil<O, SPONGE, MODE><<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.ring, pm.tile, t.amap, t, a);
+    k_stencil<O, SPONGE, MODE, DIRECT>
+        <<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.tile, cm.win, pm.tile, t.amap, t, a);
 }
 
-template <int O>
-cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, int mode, cudaStream_t s)
+template <int O, bool DIRECT>
+cudaError_t launch_of(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, int mode, cudaStream_t s)
 {
     const dim3 grid(t.grid[0], t.grid[1], t.grid[2]);
     const LevelMaps &cm = t.lv[ci], &pm = t.lv[1 - ci];
     switch (mode * 2 + (sponge ? 1 : 0)) {
-    case 0: launch_om<O, false, STENCIL_PLAIN>(grid, cm, pm, t, a, s); break;
-    case 1: launch_om<O, true, STENCIL_PLAIN>(grid, cm, pm, t, a, s); break;
-    case 2: launch_om<O, false, STENCIL_RECORD_KP>(grid, cm, pm, t, a, s); break;
-    case 3: launch_om<O, true, STENCIL_RECORD_KP>(grid, cm, pm, t, a, s); break;
-    case 4: launch_om<O, false, STENCIL_GRADIENT>(grid, cm, pm, t, a, s); break;
-    case 5: launch_om<O, true, STENCIL_GRADIENT>(grid, cm, pm, t, a, s); break;
+    case 0: launch_om<O, false, STENCIL_PLAIN, DIRECT>(grid, cm, pm, t, a, s); break;
+    case 1: launch_om<O, true, STENCIL_PLAIN, DIRECT>(grid, cm, pm, t, a, s); break;
+    case 2: launch_om<O, false, STENCIL_RECORD_KP, DIRECT>(grid, cm, pm, t, a, s); break;
+    case 3: launch_om<O, true, STENCIL_RECORD_KP, DIRECT>(grid, cm, pm, t, a, s); break;
+    case 4: launch_om<O, false, STENCIL_GRADIENT, DIRECT>(grid, cm, pm, t, a, s); break;
+    case 5: launch_om<O, true, STENCIL_GRADIENT, DIRECT>(grid, cm, pm, t, a, s); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
-template <int O, bool SPONGE, int MODE>
+template <int O>
+cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, int mode, bool direct,
+                     cudaStream_t s)
+{
+    return direct ? launch_of<O, true>(t, a, ci, sponge, mode, s) : launch_of<O, false>(t, a, ci, sponge, mode, s);
+}
+
+template <int O, bool SPONGE, int MODE, bool DIRECT>
 cudaError_t setup_om()
 {
-    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE, DIRECT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)Cfg<O>::SMEM);
+}
+
+template <int O, bool DIRECT>
+cudaError_t setup_of()
+{
+    cudaError_t e;
+    if ((e = setup_om<O, true, STENCIL_PLAIN, DIRECT>()) != cudaSuccess) return e;
+    if ((e = setup_om<O, false, STENCIL_PLAIN, DIRECT>()) != cudaSuccess) return e;
+    if ((e = setup_om<O, true, STENCIL_RECORD_KP, DIRECT>()) != cudaSuccess) return e;
+    if ((e = setup_om<O, false, STENCIL_RECORD_KP, DIRECT>()) != cudaSuccess) return e;
+    if ((e = setup_om<O, true, STENCIL_GRADIENT, DIRECT>()) != cudaSuccess) return e;
+    return setup_om<O, false, STENCIL_GRADIENT, DIRECT>();
 }
 
 template <int O>
 cudaError_t setup_o()
 {
-    cudaError_t e;
-    if ((e = setup_om<O, true, STENCIL_PLAIN>()) != cudaSuccess) return e;
-    if ((e = setup_om<O, false, STENCIL_PLAIN>()) != cudaSuccess) return e;
-    if ((e = setup_om<O, true, STENCIL_RECORD_KP>()) != cudaSuccess) return e;
-    if ((e = setup_om<O, false, STENCIL_RECORD_KP>()) != cudaSuccess) return e;
-    if ((e = setup_om<O, true, STENCIL_GRADIENT>()) != cudaSuccess) return e;
-    return setup_om<O, false, STENCIL_GRADIENT>();
+    cudaError_t e = setup_of<O, true>();
+    return e != cudaSuccess ? e : setup_of<O, false>();
 }
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -494,7 +554,8 @@ int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, Stenc
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    per_sm = std::max(1, std::min(2048 / threads, smem_sm / (int)(t->smem + 1024)));
+    per_sm = blocks_per_sm(b.order);  // kernel attributes are set up with the solver
+    if (per_sm <= 0) per_sm = std::max(1, std::min(2048 / threads, smem_sm / (int)(t->smem + 1024)));
     const int64_t cols = (int64_t)t->grid[0] * t->grid[1];
     const int64_t resident = (int64_t)sms * per_sm;
     double best = 1e300;
@@ -517,7 +578,7 @@ int stencil_bind(StencilTables &t, const float *p0, const float *p1, const float
     const int txp = t.tile_x + 2 * t.halo_x;
     const float *ps[2] = {p0, p1};
     for (int i = 0; i < 2; i++) {
-        if (!make_map(t.lv[i].ring, ps[i], t, txp, t.tile_z + 2 * t.order) ||
+        if (!make_map(t.lv[i].win, ps[i], t, txp, t.tile_z + 2 * t.order) ||
             !make_map(t.lv[i].tile, ps[i], t, t.tile_x, t.tile_z))
             return (int)cudaErrorInvalidValue;
     }
@@ -574,7 +635,16 @@ cudaError_t stencil_kernel_setup()
     for (int o = 1; o <= kMaxOrder; o++) {
         Gll g;
         gll_tables(o, g);
-        stencil_table(g, all.data() + (o - 1) * kTMax);
+        float *T = all.data() + (o - 1) * kTMax;
+        stencil_table(g, T);
+        // diagonal entry: minus the sum of the row's float coefficients, rounded once, so that
+        // the float row sums to zero up to that rounding (used by the direct form)
+        for (int l = 0; l < o; l++) {
+            double sum = 0;
+            for (int d = -o; d <= o; d++)
+                if (d != 0) sum += T[l * (2 * o + 1) + d + o];
+            T[l * (2 * o + 1) + o] = (float)-sum;
+        }
         for (int l = 0; l < o; l++) wa[(o - 1) * kMaxOrder + l] = (float)(l == 0 ? g.w[0] + g.w[o] : g.w[l]);
     }
     if ((e = cudaMemcpyToSymbol(c_T, all.data(), all.size() * sizeof(float))) != cudaSuccess) return e;
@@ -589,15 +659,15 @@ cudaError_t stencil_kernel_setup()
 }
 
 cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, int cur_index, bool sponge, cudaStream_t s,
-                           int mode)
+                           int mode, bool direct)
 {
     if (mode != STENCIL_PLAIN && (!a.kp || (mode == STENCIL_GRADIENT && !a.grad))) return cudaErrorInvalidValue;
     switch (t.order) {
-    case 1: return launch_o<1>(t, a, cur_index, sponge, mode, s);
-    case 2: return launch_o<2>(t, a, cur_index, sponge, mode, s);
-    case 3: return launch_o<3>(t, a, cur_index, sponge, mode, s);
-    case 4: return launch_o<4>(t, a, cur_index, sponge, mode, s);
-    case 5: return launch_o<5>(t, a, cur_index, sponge, mode, s);
+    case 1: return launch_o<1>(t, a, cur_index, sponge, mode, direct, s);
+    case 2: return launch_o<2>(t, a, cur_index, sponge, mode, direct, s);
+    case 3: return launch_o<3>(t, a, cur_index, sponge, mode, direct, s);
+    case 4: return launch_o<4>(t, a, cur_index, sponge, mode, direct, s);
+    case 5: return launch_o<5>(t, a, cur_index, sponge, mode, direct, s);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -15,6 +15,7 @@ struct sem_solver {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int kernel = SEM_KERNEL_AUTO;
+    int form = SEM_FORM_DIRECT;  // operator form of the stencil pass
     int64_t n_int = 0;               // nodes of the device layout
     float *d_p[2] = {nullptr, nullptr};
     int cur = 0;                 // index of the current level

@@ -21,7 +21,7 @@ namespace semgb {
 
 // Tensor maps of one pressure buffer (3-D tiles of the device layout).
 struct LevelMaps {
-    CUtensorMap ring;   // (tile width + x halo) x (TZ + 2o rows) x 1 plane
+    CUtensorMap win;    // (tile width + x halo) x (TZ + 2o rows) x 1 plane
     CUtensorMap tile;   // tile width x TZ rows x 1 plane
 };
 
@@ -74,7 +74,10 @@ cudaError_t stencil_set_receivers(StencilTables &t, const int64_t *sorted_nodes,
 void stencil_tables_free(StencilTables *&t);
 cudaError_t stencil_kernel_setup();
 // cur_index: which of the bound pressure buffers is the current level.
+// direct: operator form sum_d T_d p_{i+d} with the diagonal T_0 = -sum_{d!=0} T_d (fewer
+// instructions); otherwise the difference form sum_{d!=0} T_d (p_{i+d} - p_i), exactly zero on a
+// constant field.
 cudaError_t launch_stencil(const StencilTables &t, const StencilArgs &a, int cur_index, bool sponge,
-                           cudaStream_t s, int mode = STENCIL_PLAIN);
+                           cudaStream_t s, int mode = STENCIL_PLAIN, bool direct = true);
 
 }  // namespace semgb

@@ -20,6 +20,7 @@ LIB_PATH = os.environ.get("SEMGB_LIBRARY") or os.path.join(_HERE, "_lib", "libse
 
 SEM_OK, SEM_ERR_ARG, SEM_ERR_CUDA, SEM_ERR_OOM, SEM_ERR_TIMEOUT, SEM_ERR_UNSTABLE, SEM_ERR_STATE = range(7)
 KERNEL_AUTO, KERNEL_ELEMENT, KERNEL_STENCIL = 0, 1, 2
+FORM_DIRECT, FORM_DIFFERENCE = 0, 1
 LEVEL_CURRENT, LEVEL_PREVIOUS = 0, 1
 
 _I64P = C.POINTER(C.c_int64)
@@ -56,6 +57,7 @@ _SIGS = {
     "sem_solver_destroy": [_VP],
     "sem_solver_set_stream": [_VP, _VP],
     "sem_solver_set_kernel": [_VP, C.c_int],
+    "sem_solver_set_operator_form": [_VP, C.c_int],
     "sem_solver_set_sponge": [_VP, C.c_int, C.c_float],
     "sem_solver_set_sponge_profile": [_VP, _F32P, _F32P, _F32P],
     "sem_solver_set_sources": [_VP, C.c_int, _I64P, _F32P, C.c_int],
@@ -288,6 +290,10 @@ class Solver:
 
     def set_kernel(self, kernel: int):
         _check(lib().sem_solver_set_kernel(self._h, kernel))
+
+    def set_operator_form(self, form: int):
+        """FORM_DIRECT (default, fastest) or FORM_DIFFERENCE (exact on constant fields)."""
+        _check(lib().sem_solver_set_operator_form(self._h, form))
 
     def set_sponge(self, thickness: int, sigma: float):
         _check(lib().sem_solver_set_sponge(self._h, thickness, sigma))

@@ -30,12 +30,21 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / d) if d > 0 else float(np.linalg.norm(a - b))
 
 
+# kernel variants: the element path, and the stencil pass in its two operator forms
+KERNELS = ["element", "stencil", "stencil-difference"]
+
+
+def configure(semgb, s, kernel):
+    s.set_kernel(semgb.KERNEL_ELEMENT if kernel == "element" else semgb.KERNEL_STENCIL)
+    s.set_operator_form(semgb.FORM_DIFFERENCE if kernel == "stencil-difference" else semgb.FORM_DIRECT)
+
+
 def solver_for_fixture(semgb, f, kernel):
     mesh = semgb.Mesh(int(f["ex"]), int(f["ey"]), int(f["ez"]), float(f["lx"]), float(f["ly"]),
                       float(f["lz"]), int(f["order"]))
     mesh.set_velocity(f["vel"])
     s = semgb.Solver(mesh, float(f["dt"]))
-    s.set_kernel(kernel)
+    configure(semgb, s, kernel)
     if "sx" in f:
         s.set_sponge_profile(f["sx"], f["sy"], f["sz"])
     s.set_sources(f["src_elem"], f["wavelet"])
@@ -43,13 +52,12 @@ def solver_for_fixture(semgb, f, kernel):
     return mesh, s
 
 
-@pytest.mark.parametrize("kernel", ["element", "stencil"])
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(g)[:-4] for g in GOLDEN])
 def test_against_reference_fixture(semgb_lib, cuda_device, path, kernel):
     semgb = semgb_lib
     f = np.load(path)
-    k = semgb.KERNEL_ELEMENT if kernel == "element" else semgb.KERNEL_STENCIL
-    mesh, s = solver_for_fixture(semgb, f, k)
+    mesh, s = solver_for_fixture(semgb, f, kernel)
     s.step(int(f["nsteps"]))
     s.synchronize()
     tr = s.traces()
@@ -80,7 +88,7 @@ def test_connectivity_bit_exact(semgb_lib, cuda_device):
 
 
 @pytest.mark.parametrize("order", [1, 2, 3, 4, 5])
-@pytest.mark.parametrize("kernel", ["element", "stencil"])
+@pytest.mark.parametrize("kernel", KERNELS)
 def test_single_step_vs_oracle(semgb_lib, cuda_device, order, kernel):
     """One step from the same random smooth state: GPU vs the oracle (FP32 and FP64)."""
     from oracle import oracle as O
@@ -102,7 +110,7 @@ def test_single_step_vs_oracle(semgb_lib, cuda_device, order, kernel):
     mesh = semgb.Mesh(wl.ex, wl.ey, wl.ez, wl.lx, wl.ly, wl.lz, o)
     mesh.set_velocity(wl.vel)
     s = semgb.Solver(mesh, wl.dt)
-    s.set_kernel(semgb.KERNEL_ELEMENT if kernel == "element" else semgb.KERNEL_STENCIL)
+    configure(semgb, s, kernel)
     s.set_sponge_profile(*P.sponge32)
     s.set_sources(P.src_elem, P.wavelet)
     s.set_receiver_nodes(P.rec_node)
@@ -191,3 +199,45 @@ def test_cpp_driver_matches_oracle(semgb_lib, cuda_device):
     _, _, tr = O.run(P)
     ref = tr[[0, 100, 200], 0]
     assert np.allclose(vals, ref, rtol=1e-4, atol=1e-6 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("order", [2, 3, 4])
+def test_operator_forms_on_a_constant_field(semgb_lib, cuda_device, order):
+    """A constant field with no source and no sponge is a solution: the difference form keeps it
+    bit for bit (every term is exactly zero); the direct form's float row sums leave at most a
+    rounding-level drift."""
+    from semgb import workloads as W
+    semgb = semgb_lib
+    mesh = semgb.Mesh(6, 5, 4, 60.0, 50.0, 40.0, order)
+    mesh.set_velocity(np.full(6 * 5 * 4, 2000.0, np.float32))
+    const = np.full(mesh.n_nodes, 0.7310585, np.float32)
+    for form in (semgb.FORM_DIFFERENCE, semgb.FORM_DIRECT):
+        s = semgb.Solver(mesh, W.cfl_dt(10.0, order, 2000.0))
+        s.set_kernel(semgb.KERNEL_STENCIL)
+        s.set_operator_form(form)
+        s.set_pressure(semgb.LEVEL_CURRENT, const)
+        s.set_pressure(semgb.LEVEL_PREVIOUS, const)
+        s.step(25)
+        p = s.pressure()
+        if form == semgb.FORM_DIFFERENCE:
+            assert np.array_equal(p, const)
+        else:
+            assert rel_l2(p, const) < 1e-5
+        s.close()
+
+
+def test_operator_forms_agree(semgb_lib, cuda_device):
+    """The two forms of the stencil pass evaluate the same operator: traces and fields agree to
+    FP32 rounding drift over 120 steps."""
+    from semgb import workloads as W
+    semgb = semgb_lib
+    wl = W.small_random(10, 9, 8, 4, 120, seed=78, nsrc=2, nrec=16)
+    res = []
+    for form in (semgb.FORM_DIRECT, semgb.FORM_DIFFERENCE):
+        mesh, s = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
+        s.set_operator_form(form)
+        s.step(120)
+        res.append((s.traces(), s.pressure()))
+    assert rel_l2(res[0][0], res[1][0]) < 1e-5
+    assert rel_l2(res[0][1], res[1][1]) < 1e-5
+    assert not np.array_equal(res[0][1], res[1][1])  # the form switch took effect
