@@ -118,15 +118,15 @@ struct VecO {
 };
 
 // Axis term along a direction whose local index LOC is uniform over the thread's O nodes:
-// r[j] = sum_d T[LOC][d] (row(d)[j] - c[j]).  row(d) returns the pointer to the O values at
-// offset d along the axis.
+// direct form r[j] = sum_d T[LOC][d] row(d)[j] (diagonal included), difference form
+// r[j] = sum_{d!=0} T[LOC][d] (row(d)[j] - c[j]).  row(d) returns the pointer to the O values
+// at offset d along the axis.
 template <int O, int LOC, bool DIRECT, class RowFn>
 __device__ __forceinline__ VecO<O> axis_uniform(const float (&c)[O], const RowFn &row)
 {
     VecO<O> r;
     if constexpr (DIRECT) {
-        // direct form: diagonal T[LOC][o] times the node, then one fma per neighbour; the
-        // coefficients are constant-bank operands of scalar fmas
+        // the coefficients are constant-bank operands of scalar fmas
 #pragma unroll
         for (int j = 0; j < O; j++) r.v[j] = c_T[O - 1][LOC * (2 * O + 1) + O] * c[j];
 #pragma unroll
@@ -137,29 +137,30 @@ __device__ __forceinline__ VecO<O> axis_uniform(const float (&c)[O], const RowFn
 #pragma unroll
             for (int j = 0; j < O; j++) r.v[j] = fmaf(c_T[O - 1][LOC * (2 * O + 1) + d + O], v[j], r.v[j]);
         }
-        return r;
-    }
+    } else {
 #pragma unroll
-    for (int j = 0; j < O; j++) r.v[j] = 0.f;
+        for (int j = 0; j < O; j++) r.v[j] = 0.f;
 #pragma unroll
-    for (int d = dlo(O, LOC); d <= dhi(O, LOC); d++) {
-        if (d == 0) continue;
-        float v[O];
-        load_o<O>(row(d), v);
-        const float t = c_T[O - 1][LOC * (2 * O + 1) + d + O];
-        if constexpr (O % 2 == 0) {
-            // the coefficient is shared by the thread's nodes: pairs of nodes in packed f32x2
-            // (each half rounds as the scalar sub and fma would)
+        for (int d = dlo(O, LOC); d <= dhi(O, LOC); d++) {
+            if (d == 0) continue;
+            float v[O];
+            load_o<O>(row(d), v);
+            const float t = c_T[O - 1][LOC * (2 * O + 1) + d + O];
+            if constexpr (O % 2 == 0) {
+                // the coefficient is shared by the thread's nodes: pairs of nodes in packed f32x2
+                // (each half rounds as the scalar sub and fma would)
 #pragma unroll
-            for (int j = 0; j < O; j += 2) {
-                const float2 acc = fma2(make_float2(t, t), sub2(make_float2(v[j], v[j + 1]), make_float2(c[j], c[j + 1])),
-                                        make_float2(r.v[j], r.v[j + 1]));
-                r.v[j] = acc.x;
-                r.v[j + 1] = acc.y;
+                for (int j = 0; j < O; j += 2) {
+                    const float2 acc = fma2(make_float2(t, t),
+                                            sub2(make_float2(v[j], v[j + 1]), make_float2(c[j], c[j + 1])),
+                                            make_float2(r.v[j], r.v[j + 1]));
+                    r.v[j] = acc.x;
+                    r.v[j + 1] = acc.y;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < O; j++) r.v[j] = fmaf(t, v[j] - c[j], r.v[j]);
             }
-        } else {
-#pragma unroll
-            for (int j = 0; j < O; j++) r.v[j] = fmaf(t, v[j] - c[j], r.v[j]);
         }
     }
     return r;
@@ -185,16 +186,17 @@ struct ZRows {
     __device__ __forceinline__ const float *operator()(int d) const { return base + d * txp; }
 };
 
-// y-neighbour rows: ring slot of plane y+d (slot index of plane y is `slot`, ring of `r`).
+// y-neighbour rows: ring slot of plane y+d.  `base` points into the slot of plane y (index
+// `slot` of R slots of SF floats); wrapping around the ring selects one of two precomputed
+// bases, the offset d*SF being an immediate of the load.
+template <int R, int SF>
 struct YPlanes {
-    const float *ring;
-    int slot, r, slot_floats, off;
+    const float *base, *base_lo, *base_hi;  // base, base + R*SF, base - R*SF
+    int slot;
     __device__ __forceinline__ const float *operator()(int d) const
     {
-        int i = slot + d;
-        if (d > 0) i = i >= r ? i - r : i;
-        if (d < 0) i = i < 0 ? i + r : i;
-        return ring + i * slot_floats + off;
+        if (d > 0) return (slot >= R - d ? base_hi : base) + d * SF;
+        return (slot < -d ? base_lo : base) + d * SF;
     }
 };
 
@@ -210,7 +212,6 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     float *ring = reinterpret_cast<float *>(smem);
     float *aux = reinterpret_cast<float *>(smem + C::OFF_AUX);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + C::OFF_BAR);  // [R] ring, [AUX] aux
-    __shared__ int s_abort;
 
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
@@ -235,7 +236,6 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     };
 
     if (threadIdx.x == 0) {
-        s_abort = 0;
         for (int i = 0; i < R + AUX; i++) bar_init(bars + i, 1);
         fence_barrier_init();
     }
@@ -269,23 +269,30 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
         const int i = p - yb + O;  // < 2O < R: first fill of each of these slots
         ok &= bar_wait(bars + i, 0, kWaitLimitNs);
     }
-    if (!ok) { s_abort = 1; atomicExch(a.status, 1); }
+    if (!ok) atomicExch(a.status, 1);
+    bool aborted = __syncthreads_or(!ok) != 0;
 
-    int rs = O;     // ring slot of plane y
-    int as = 0;     // aux slot of plane y
+    // all O nodes of the thread strictly inside the mesh along x: no per-node checks on the
+    // common path
+    const bool xall = xb > 0 && xb + O < nx;
+    float sxz[O];  // (sx*sz) of the thread's nodes; the node factor is (sx*sz)*sy
+#pragma unroll
+    for (int j = 0; j < O; j++) sxz[j] = sxv[j] * szv;
+
+    int rs = O;         // ring slot of plane y
+    int ws = 2 * O;     // ring slot of plane y+O, the one waited for (2O < R), and its phase
+    uint32_t wph = 0;
+    int as = 0;         // aux slot of plane y and its phase
+    uint32_t aph = 0;
     int ly = yb % O;
-    for (int y = yb; y < ye; y++) {
+    for (int y = yb; y < ye && !aborted; y++) {
         if (threadIdx.x == 0 && y + kLook <= ye - 1) {
             issue_ring(y + O + kLook);
             issue_aux(y + kLook);
         }
-        {
-            const int pr = y + O - yb + O;  // fill index of ring plane y+O
-            const int pa = y - yb;
-            ok = bar_wait(bars + pr % R, (uint32_t)((pr / R) & 1), kWaitLimitNs);
-            ok &= bar_wait(bars + R + as, (uint32_t)((pa / AUX) & 1), kWaitLimitNs);
-            if (!ok) { s_abort = 1; atomicExch(a.status, 1); }
-        }
+        ok = bar_wait(bars + ws, wph, kWaitLimitNs);
+        ok &= bar_wait(bars + R + as, aph, kWaitLimitNs);
+        if (!ok) atomicExch(a.status, 1);
         if (row_ok) {
             const float *cur = aux + as * C::AUX_FLOATS + 2 * C::TILE_FLOATS + off;  // window
             const float *tq = aux + as * C::AUX_FLOATS + toff;
@@ -313,7 +320,9 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
                 ax[j] = acc;
             }
             const VecO<O> az = axis_dispatch<O, DIRECT>(lz, c, ZRows{cur, TXP});
-            const VecO<O> ay = axis_dispatch<O, DIRECT>(ly, c, YPlanes{ring, rs, R, C::RING_FLOATS, toff});
+            const float *yb0 = ring + rs * C::RING_FLOATS + toff;
+            const YPlanes<R, C::RING_FLOATS> yrows{yb0, yb0 + R * C::RING_FLOATS, yb0 - R * C::RING_FLOATS, rs};
+            const VecO<O> ay = axis_dispatch<O, DIRECT>(ly, c, yrows);
 
             const bool yin = y > 0 && y < ny - 1;
             const float wy = c_wa[O - 1][ly];
@@ -322,19 +331,32 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
             float out[O], kp[O];
             if (MODE == STENCIL_GRADIENT)
                 load_o_lim<O>(a.kp + (dst_col - a.prev) + (int64_t)y * plane_stride, kp, (int)t.nxp - xb);
+            float sv[O], qdv[O];
 #pragma unroll
             for (int j = 0; j < O; j++) {
                 const float wxj = c_wa[O - 1][j];
-                const float s = SPONGE ? sxv[j] * syv * szv : 1.f;  // (sx*sy)*sz
-                const float qd = SPONGE ? s * q[j] : q[j];
-                float v = qd;
-                if (MODE == STENCIL_RECORD_KP) kp[j] = 0.f;
-                if (xb + j > 0 && xb + j < nx - 1 && zin && yin) {
-                    const float yv = gx * ax[j] + (gzy * wxj) * az.v[j] + (gyz * wxj) * ay.v[j];
-                    v = (2.f * c[j] - qd) - am[j] * yv;
-                    if (MODE == STENCIL_RECORD_KP) kp[j] = yv;
+                sv[j] = SPONGE ? sxz[j] * syv : 1.f;
+                qdv[j] = SPONGE ? sv[j] * q[j] : q[j];
+                // K.p at the node: g1 Wz Wy A_x + Wx (g2 Wy A_z + g3 Wz A_y)
+                const float yv = fmaf(wxj, fmaf(gyz, ay.v[j], gzy * az.v[j]), gx * ax[j]);
+                out[j] = (2.f * c[j] - qdv[j]) - am[j] * yv;
+                if (MODE == STENCIL_RECORD_KP) kp[j] = yv;
+            }
+            if (!(xall && zin && yin)) {
+                // boundary and padding nodes: no update (the stored previous level is kept, then
+                // damped), padding columns stay zero
+#pragma unroll
+                for (int j = 0; j < O; j++) {
+                    if (!(xb + j > 0 && xb + j < nx - 1 && zin && yin)) {
+                        out[j] = qdv[j];
+                        if (MODE == STENCIL_RECORD_KP) kp[j] = 0.f;
+                    }
                 }
-                out[j] = xb + j < nx ? (SPONGE ? s * v : v) : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < O; j++) {
+                if (SPONGE) out[j] = sv[j] * out[j];
+                if (!xall && xb + j >= nx) out[j] = 0.f;
             }
             float *dst = dst_col + (int64_t)y * plane_stride;
             if (MODE != STENCIL_PLAIN) {
@@ -361,14 +383,14 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
                     if (xb + j < t.nxp) dst[j] = out[j];
             }
         }
-        __syncthreads();
-        if (s_abort) break;
+        aborted = __syncthreads_or(!ok) != 0;
         rs = rs + 1 == R ? 0 : rs + 1;
-        as = as + 1 == AUX ? 0 : as + 1;
+        if (++ws == R) { ws = 0; wph ^= 1; }
+        if (++as == AUX) { as = 0; aph ^= 1; }
         ly = ly + 1 == O ? 0 : ly + 1;
     }
 
-    if (s_abort) {
+    if (aborted) {
         // leave no copy in flight into this CTA's shared memory: bounded drain of every barrier
         if (threadIdx.x == 0)
             for (int i = 0; i < R + AUX; i++) {
