@@ -214,8 +214,10 @@ int sem_solver_time_kernels(sem_solver *s, int n_steps, float *ms);
 /* ------------------------------------------------------------------------------------------
  * Many shots on one mesh (batched form).  The reference runs one source per process
  * (SEMdata.hpp:13, SEMproxy.cpp:93-119); a batch advances n_shots independent shots that share
- * the mesh, the velocity model, the sponge and the receiver set, with the shot index innermost
- * in memory so that all mesh-side work and data are shared.  Same conventions as sem_solver_*.
+ * the mesh, the velocity model, the sponge and the receiver set.  The shots' fields lie one
+ * after another and one stencil pass steps them all, the CTAs of every shot of a tile running
+ * together so that the mesh-side data (dt^2/M, sponge) is read from memory once per tile for
+ * the batch.  Same conventions as sem_solver_*.
  * ------------------------------------------------------------------------------------------ */
 
 typedef struct sem_batch sem_batch;
@@ -239,8 +241,9 @@ int sem_batch_get_traces(sem_batch *b, float *out);
 int sem_batch_get_pressure(sem_batch *b, int shot, int level, float *out);
 /* Time n_steps (CUDA events on the batch's stream); advances the batch. */
 int sem_batch_time_step(sem_batch *b, int n_steps, float *ms_per_step);
-/* Time the candidate launch shapes (shots per lane, x-columns per CTA, planes per CTA) on the
- * current state, keep the fastest, restore the state; any output pointer may be NULL. */
+/* Time the candidate launch shapes (planes per CTA along y; one shot per CTA and 8 warps per CTA
+ * are fixed) on the current state, keep the fastest, restore the state; any output pointer may
+ * be NULL. */
 int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, int *ychunk);
 
 /* ------------------------------------------------------------------------------------------

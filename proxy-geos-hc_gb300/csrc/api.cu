@@ -546,7 +546,7 @@ int solver_prepare(sem_solver *s, int64_t n_new)
         }
     } else {
         if (!s->stencil) {
-            int rc = stencil_tables_create(m->box, m->gll, m->geo, &s->stencil);
+            int rc = stencil_tables_create(m->box, m->gll, m->geo, 1, &s->stencil);
             if (rc) return fail(SEM_ERR_CUDA, "stencil tables");
         }
         if (stencil_bind(*s->stencil, s->d_p[0], s->d_p[1], s->d_a) != 0)

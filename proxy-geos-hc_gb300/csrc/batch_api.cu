@@ -1,6 +1,9 @@
 // batch_api.cu -- C ABI of the many-shot form (sem_batch_*): shots that share one mesh, model,
-// sponge and receiver set advance together (k_batch.cu); the time loop is replayed from a
-// captured CUDA graph and the launch shape is picked by a timing autotuner.
+// sponge and receiver set advance together.  The levels hold the shots' fields one after
+// another and one stencil pass (k_stencil.cu, nshot > 1) steps them all: the CTAs of all shots
+// of a tile run together, so each dt^2/M plane comes from DRAM once for the batch (12 + 4/S
+// bytes per shot-node-step against 16).  The time loop is replayed from a captured CUDA graph;
+// the autotuner times the y-chunk length.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -10,6 +13,7 @@
 
 #include "abi.h"
 #include "batch.h"
+#include "stencil.h"
 
 using namespace semgb;
 
@@ -17,11 +21,10 @@ struct sem_batch {
     sem_mesh *mesh = nullptr;
     float dt = 0;
     int nshot = 0;
-    int64_t s_pad = 0;
-    int64_t n_int = 0;
+    int64_t n_int = 0;  // floats per shot field (device layout)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    float *d_p[2] = {nullptr, nullptr};  // [n_int][s_pad]
+    float *d_p[2] = {nullptr, nullptr};  // [nshot][n_int]: the shots' fields one after another
     int cur = 0;
     float *d_a = nullptr;
     uint64_t a_version = 0;
@@ -33,11 +36,16 @@ struct sem_batch {
     float *d_src_coef = nullptr;
     float *d_wavelet = nullptr;
     int nrec = 0;
+    std::vector<int64_t> rec_sorted;  // device-layout nodes, sorted
     int64_t *d_rec_node = nullptr;
+    int *d_rec_perm = nullptr;
+    uint64_t rec_version = 0;
     float *d_traces = nullptr;  // [cap][nrec][nshot]
     int64_t trace_cap = 0;
     int *d_ctr = nullptr;
+    int *d_status = nullptr;
     int64_t steps_done = 0;
+    StencilTables *st = nullptr;
     BatchTuning tune;
     bool tuned = false;
     cudaGraphExec_t graph2[2] = {nullptr, nullptr};
@@ -51,49 +59,39 @@ void invalidate(sem_batch *b)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
 }
 
-bool tables_uploaded = false;
-
-cudaError_t ensure_tables()
+StencilArgs args_for(const sem_batch *b, int c, bool record)
 {
-    if (tables_uploaded) return cudaSuccess;
-    constexpr int kT = kMaxOrder * (2 * kMaxOrder + 1);
-    std::vector<float> T(kMaxOrder * kT, 0.f), wa(kMaxOrder * kMaxOrder, 0.f);
-    for (int o = 1; o <= kMaxOrder; o++) {
-        Gll g;
-        gll_tables(o, g);
-        stencil_table(g, T.data() + (o - 1) * kT);
-        for (int l = 0; l < o; l++) wa[(o - 1) * kMaxOrder + l] = (float)(l == 0 ? g.w[0] + g.w[o] : g.w[l]);
-    }
-    cudaError_t e = batch_kernel_setup(T.data(), wa.data());
-    if (e == cudaSuccess) tables_uploaded = true;
-    return e;
-}
-
-BatchArgs args_for(const sem_batch *b, int c)
-{
-    const Box &x = b->mesh->box;
-    BatchArgs a{};
+    StencilArgs a{};
     a.cur = b->d_p[c];
     a.prev = b->d_p[1 - c];
-    a.a = b->d_a;
     a.sx = b->d_sx; a.sy = b->d_sy; a.sz = b->d_sz;
-    a.nx = x.nx; a.nxp = x.nxp; a.ny = x.ny; a.nz = x.nz;
-    a.s_pad = b->s_pad;
-    a.ychunk = b->tune.ychunk > 0 ? b->tune.ychunk : (int)x.ny;
-    for (int d = 0; d < 3; d++) a.g[d] = (float)b->mesh->geo.g[d];
+    a.rec_node = b->d_rec_node;
+    a.rec_perm = b->d_rec_perm;
+    a.rec_off = b->st->d_rec_off;
+    a.rec_idx = b->st->d_rec_idx;
+    a.nrec = record ? b->nrec : 0;
+    a.traces = b->d_traces;
+    a.ctr = b->d_ctr;
+    a.status = b->d_status;
     return a;
 }
 
 cudaError_t enqueue(sem_batch *b, int c)
 {
     BatchSourceArgs sa{b->d_p[c], b->d_src_node, b->d_src_coef, b->d_wavelet, b->nsamples > 0 ? b->nshot : 0,
-                       b->nsamples, b->s_pad, b->d_ctr};
+                       b->nsamples, b->n_int, b->d_ctr};
     cudaError_t e = launch_batch_source(sa, b->d_ctr, b->stream);
     if (e != cudaSuccess) return e;
-    e = launch_batch_step(b->mesh->box.order, args_for(b, c), b->sponge, b->tune, b->stream);
-    if (e != cudaSuccess) return e;
-    BatchRecordArgs ra{b->d_p[1 - c], b->d_rec_node, b->nrec, b->nshot, b->s_pad, b->d_traces, b->d_ctr};
-    return launch_batch_record(ra, b->stream);
+    return launch_stencil(*b->st, args_for(b, c, true), c, b->sponge, b->stream);
+}
+
+// Sets the stencil pass's y-chunk (planes per CTA) and regroups the receivers by CTA.
+cudaError_t set_chunk(sem_batch *b, int ychunk)
+{
+    StencilTables &t = *b->st;
+    t.ychunk = std::max(1, std::min<int>(ychunk, (int)t.ny));
+    t.grid[2] = (int)((t.ny + t.ychunk - 1) / t.ychunk);
+    return stencil_set_receivers(t, b->rec_sorted.data(), b->nrec, b->rec_version);
 }
 
 int prepare(sem_batch *b, int64_t n_new)
@@ -103,6 +101,12 @@ int prepare(sem_batch *b, int64_t n_new)
         CUDA_TRY(launch_mass(b->d_a, m->d_slow2 ? nullptr : m->d_vel, m->d_slow2, m->box.ex, m->box.ey, m->box.ez,
                              m->box.order, m->box.nxp, b->d_w, m->geo.detJ, (double)b->dt * b->dt, b->stream));
         b->a_version = m->model_version;
+    }
+    if (stencil_bind(*b->st, b->d_p[0], b->d_p[1], b->d_a) != 0)
+        return sem_fail(SEM_ERR_CUDA, "tensor-map encoding failed (driver entry point cuTensorMapEncodeTiled)");
+    if (b->st->rec_version != b->rec_version) {
+        CUDA_TRY(stencil_set_receivers(*b->st, b->rec_sorted.data(), b->nrec, b->rec_version));
+        invalidate(b);
     }
     if (b->nrec > 0 && b->steps_done + n_new > b->trace_cap) {
         const int64_t cap = std::max<int64_t>(b->steps_done + n_new, std::max<int64_t>(64, 2 * b->trace_cap));
@@ -121,23 +125,16 @@ int prepare(sem_batch *b, int64_t n_new)
     return SEM_OK;
 }
 
-// Launch shapes the autotuner tries: whole columns or y-chunks of about a half, a quarter or an
-// eighth of the planes (whole elements; the carried partial sum costs one extra element of
-// loads per chunk).  The CTA is fixed at 8 z-rows of one element span.
-std::vector<BatchTuning> candidates(const sem_batch *b)
+// y-chunk lengths the autotuner tries: the stencil pass's own choice (it balances waves from the
+// measured occupancy) and whole columns, halves and quarters.
+std::vector<int> candidates(const sem_batch *b, int own)
 {
-    std::vector<BatchTuning> v;
-    const int64_t ny = b->mesh->box.ny, o = b->mesh->box.order;
-    for (int wpc : {8})
-        for (int64_t div : {1, 2, 4, 8}) {
-            const int64_t chunk = ((ny + div - 1) / div + o - 1) / o * o;
-            if (div > 1 && chunk < 8 * o) continue;
-            BatchTuning t;
-            t.shots_per_lane = 1;
-            t.warps_per_cta = wpc;
-            t.ychunk = (int)(div == 1 ? ny : chunk);
-            v.push_back(t);
-        }
+    const int ny = (int)b->mesh->box.ny;
+    std::vector<int> v{own};
+    for (int div : {1, 2, 4}) {
+        const int c = (ny + div - 1) / div;
+        if (std::find(v.begin(), v.end(), c) == v.end()) v.push_back(c);
+    }
     return v;
 }
 
@@ -156,8 +153,11 @@ int sem_batch_destroy(sem_batch *b)
     dfree(b->d_sx); dfree(b->d_sy); dfree(b->d_sz);
     dfree(b->d_src_node); dfree(b->d_src_coef); dfree(b->d_wavelet);
     dfree(b->d_rec_node);
+    dfree(b->d_rec_perm);
     dfree(b->d_traces);
     dfree(b->d_ctr);
+    dfree(b->d_status);
+    stencil_tables_free(b->st);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return SEM_OK;
@@ -173,7 +173,6 @@ int sem_batch_create(sem_mesh *m, float dt, int n_shots, sem_batch **out)
     b->mesh = m;
     b->dt = dt;
     b->nshot = n_shots;
-    b->s_pad = (n_shots + 31) / 32 * 32;
     b->n_int = m->box.n_int;
     auto cleanup = [&](int code, const std::string &msg) {
         sem_batch_destroy(b);
@@ -182,7 +181,7 @@ int sem_batch_create(sem_mesh *m, float dt, int n_shots, sem_batch **out)
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     b->own_stream = true;
-    const size_t n = (size_t)b->n_int * b->s_pad;
+    const size_t n = (size_t)b->n_int * b->nshot;
     for (auto &p : b->d_p)
         if ((e = dalloc(&p, n)) != cudaSuccess || (e = cudaMemset(p, 0, n * 4)) != cudaSuccess)
             return cleanup(SEM_ERR_OOM, std::string("pressure levels: ") + cudaGetErrorString(e));
@@ -190,13 +189,16 @@ int sem_batch_create(sem_mesh *m, float dt, int n_shots, sem_batch **out)
         return cleanup(SEM_ERR_OOM, cudaGetErrorString(e));
     if ((e = dalloc(&b->d_ctr, 2)) != cudaSuccess || (e = cudaMemset(b->d_ctr, 0, 8)) != cudaSuccess)
         return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
+    if ((e = dalloc(&b->d_status, 1)) != cudaSuccess || (e = cudaMemset(b->d_status, 0, 4)) != cudaSuccess)
+        return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     if ((e = dalloc(&b->d_w, m->box.order + 1)) != cudaSuccess ||
         (e = cudaMemcpy(b->d_w, m->gll.w, (m->box.order + 1) * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
         return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
-    if ((e = ensure_tables()) != cudaSuccess) return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
+    if ((e = stencil_kernel_setup()) != cudaSuccess) return cleanup(SEM_ERR_CUDA, std::string("kernel set-up: ") + cudaGetErrorString(e));
+    if (stencil_tables_create(m->box, m->gll, m->geo, n_shots, &b->st) != 0) return cleanup(SEM_ERR_CUDA, "stencil tables");
     b->tune.shots_per_lane = 1;
     b->tune.warps_per_cta = 8;
-    b->tune.ychunk = (int)std::max<int64_t>(8 * m->box.order, (m->box.ny / 8 + m->box.order - 1) / m->box.order * m->box.order);
+    b->tune.ychunk = b->st->ychunk;
     *out = b;
     return SEM_OK;
     GUARD_END
@@ -298,20 +300,28 @@ int sem_batch_set_receiver_nodes(sem_batch *b, int n_rec, const int64_t *nodes)
     GUARD_BEGIN
     if (!b || n_rec < 0 || (n_rec > 0 && !nodes)) return sem_fail(SEM_ERR_ARG, "bad receiver array");
     if (b->steps_done > 0) return sem_fail(SEM_ERR_STATE, "receivers must be set before the first step");
-    std::vector<int64_t> q(n_rec);
-    for (int r = 0; r < n_rec; r++) {
+    for (int r = 0; r < n_rec; r++)
         if (nodes[r] < 0 || nodes[r] >= b->mesh->box.n_nodes) return sem_fail(SEM_ERR_ARG, "receiver node out of range");
-        q[r] = to_internal(b->mesh->box, nodes[r]);
-    }
+    // node-sorted (the stencil pass groups them by owning CTA); perm maps back to the caller's order
+    std::vector<int> perm(n_rec);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return nodes[x] < nodes[y]; });
+    std::vector<int64_t> sorted(n_rec);
+    for (int r = 0; r < n_rec; r++) sorted[r] = to_internal(b->mesh->box, nodes[perm[r]]);
     cudaStreamSynchronize(b->stream);
     invalidate(b);
     dfree(b->d_rec_node);
+    dfree(b->d_rec_perm);
     dfree(b->d_traces);
     b->trace_cap = 0;
     b->nrec = n_rec;
+    b->rec_sorted = sorted;
+    b->rec_version++;
     if (n_rec > 0) {
         CUDA_TRY(dalloc(&b->d_rec_node, n_rec));
-        CUDA_TRY(cudaMemcpy(b->d_rec_node, q.data(), n_rec * 8, cudaMemcpyHostToDevice));
+        CUDA_TRY(dalloc(&b->d_rec_perm, n_rec));
+        CUDA_TRY(cudaMemcpy(b->d_rec_node, sorted.data(), n_rec * 8, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(b->d_rec_perm, perm.data(), n_rec * 4, cudaMemcpyHostToDevice));
     }
     return SEM_OK;
     GUARD_END
@@ -367,6 +377,9 @@ int sem_batch_synchronize(sem_batch *b)
 {
     if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
     CUDA_TRY(cudaStreamSynchronize(b->stream));
+    int status = 0;
+    CUDA_TRY(cudaMemcpy(&status, b->d_status, 4, cudaMemcpyDeviceToHost));
+    if (status != 0) return sem_fail(SEM_ERR_TIMEOUT, "a bounded device wait gave up (TMA copy not completed)");
     return SEM_OK;
 }
 
@@ -390,11 +403,9 @@ int sem_batch_get_pressure(sem_batch *b, int shot, int level, float *out)
     const Box &x = b->mesh->box;
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     const int idx = level == SEM_LEVEL_CURRENT ? b->cur : 1 - b->cur;
-    // one shot is a strided column of [n_int][s_pad]: gather it with one 2-D copy, then drop the
-    // row padding
+    // one shot is one contiguous field of the level; drop the row padding
     std::vector<float> col((size_t)x.n_int);
-    CUDA_TRY(cudaMemcpy2D(col.data(), 4, b->d_p[idx] + shot, (size_t)b->s_pad * 4, 4, (size_t)x.n_int,
-                          cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(col.data(), b->d_p[idx] + (size_t)shot * b->n_int, (size_t)x.n_int * 4, cudaMemcpyDeviceToHost));
     int64_t i = 0;
     for (int64_t r = 0; r < x.nz * x.ny; r++)
         for (int64_t c = 0; c < x.nx; c++) out[i++] = col[(size_t)r * x.nxp + c];
@@ -439,54 +450,44 @@ int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, in
 {
     GUARD_BEGIN
     if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
-    // time every candidate on scratch copies of the current levels; the state is restored after
-    const size_t n = (size_t)b->n_int * b->s_pad;
-    std::vector<float> save0, save1;
+    // time every candidate on the current levels; a step only writes the previous level, which
+    // is saved first and restored after, and the trials record no traces
     CUDA_TRY(cudaStreamSynchronize(b->stream));
-    const int64_t steps0 = b->steps_done;
-    const int cur0 = b->cur;
-    int ctr0[2];
-    CUDA_TRY(cudaMemcpy(ctr0, b->d_ctr, 8, cudaMemcpyDeviceToHost));
-    int rc = prepare(b, 4);
+    int rc = prepare(b, 0);
     if (rc) return rc;
-    float *keep[2] = {nullptr, nullptr};
-    for (int i = 0; i < 2; i++) {
-        CUDA_TRY(dalloc(&keep[i], n));
-        CUDA_TRY(cudaMemcpyAsync(keep[i], b->d_p[i], n * 4, cudaMemcpyDeviceToDevice, b->stream));
-    }
+    const size_t n = (size_t)b->n_int * b->nshot;
+    float *keep = nullptr;
+    CUDA_TRY(dalloc(&keep, n));
+    CUDA_TRY(cudaMemcpyAsync(keep, b->d_p[1 - b->cur], n * 4, cudaMemcpyDeviceToDevice, b->stream));
     cudaEvent_t e0, e1;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
-    BatchTuning pick = b->tune;
-    for (const BatchTuning &t : candidates(b)) {
-        b->tune = t;
-        const int order = b->mesh->box.order;
-        cudaError_t err = launch_batch_step(order, args_for(b, b->cur), b->sponge, t, b->stream);  // warm-up
+    int pick = b->st->ychunk;
+    for (int chunk : candidates(b, b->st->ychunk)) {
+        cudaError_t err = set_chunk(b, chunk);
+        const StencilArgs a = args_for(b, b->cur, false);
+        if (err == cudaSuccess) err = launch_stencil(*b->st, a, b->cur, b->sponge, b->stream);  // warm-up
         cudaEventRecord(e0, b->stream);
-        for (int r = 0; r < 3 && err == cudaSuccess; r++) err = launch_batch_step(order, args_for(b, b->cur), b->sponge, t, b->stream);
+        for (int r = 0; r < 3 && err == cudaSuccess; r++) err = launch_stencil(*b->st, a, b->cur, b->sponge, b->stream);
         cudaEventRecord(e1, b->stream);
         cudaEventSynchronize(e1);
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (err == cudaSuccess && ms < best) { best = ms; pick = t; }
+        if (err == cudaSuccess && ms < best) { best = ms; pick = b->st->ychunk; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    for (int i = 0; i < 2; i++) {
-        CUDA_TRY(cudaMemcpyAsync(b->d_p[i], keep[i], n * 4, cudaMemcpyDeviceToDevice, b->stream));
-    }
+    CUDA_TRY(cudaMemcpyAsync(b->d_p[1 - b->cur], keep, n * 4, cudaMemcpyDeviceToDevice, b->stream));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
-    for (auto &k : keep) dfree(k);
-    CUDA_TRY(cudaMemcpy(b->d_ctr, ctr0, 8, cudaMemcpyHostToDevice));
-    b->steps_done = steps0;
-    b->cur = cur0;
-    b->tune = pick;
+    dfree(keep);
+    CUDA_TRY(set_chunk(b, pick));
+    b->tune.ychunk = pick;
     b->tuned = true;
     invalidate(b);
-    if (shots_per_lane) *shots_per_lane = pick.shots_per_lane;
-    if (warps_per_cta) *warps_per_cta = pick.warps_per_cta;
-    if (ychunk) *ychunk = pick.ychunk;
+    if (shots_per_lane) *shots_per_lane = b->tune.shots_per_lane;
+    if (warps_per_cta) *warps_per_cta = b->tune.warps_per_cta;
+    if (ychunk) *ychunk = pick;
     return SEM_OK;
     GUARD_END
 }

@@ -200,7 +200,7 @@ struct YPlanes {
     }
 };
 
-template <int O, bool SPONGE, int MODE, bool DIRECT>
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI>
 __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap win_map,
               const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap a_map,
@@ -214,8 +214,25 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + C::OFF_BAR);  // [R] ring, [AUX] aux
 
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
-    const int yb = blockIdx.z * t.ychunk;
+    // CTA -> (x-tile, z-tile, y-chunk): grid (x-tiles, z-tiles, chunks).  MULTI (many shots, the
+    // levels stacking the shots along y: plane p of shot s is plane s*ny + p): grid
+    // (shots * z-tiles * x-tiles, chunks) with the shot varying fastest, then z, so that the CTAs
+    // of all shots of a tile run together and share its dt^2/M planes and z-halo rows in L2.
+    int shot = 0, bx, bz, chunk;
+    if constexpr (MULTI) {
+        const int tile = (int)(blockIdx.x / (unsigned)t.nshot);
+        shot = (int)(blockIdx.x - (unsigned)tile * (unsigned)t.nshot);
+        bz = tile % t.grid[1];
+        bx = tile / t.grid[1];
+        chunk = (int)blockIdx.y;
+    } else {
+        bx = (int)blockIdx.x;
+        bz = (int)blockIdx.y;
+        chunk = (int)blockIdx.z;
+    }
+    const int x0 = bx * TX, z0 = bz * TZ;
+    const int yb = chunk * t.ychunk;
+    const int ys = MULTI ? shot * (int)t.ny : 0;  // plane offset of the shot in the stacked levels
     const int ye = (int)min((int64_t)t.ny, (int64_t)yb + t.ychunk);
     const int nx = (int)t.nx, nz = (int)t.nz, ny = (int)t.ny;
 
@@ -224,15 +241,15 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     auto issue_ring = [=](int p) {
         const int i = (p - yb + O) % R;
         bar_arrive_expect_tx(bars + i, C::RING_TX);
-        tma_load_3d(ring + i * C::RING_FLOATS, rmap, x0, z0, p, bars + i);
+        tma_load_3d(ring + i * C::RING_FLOATS, rmap, x0, z0, ys + p, bars + i);
     };
     auto issue_aux = [=](int p) {
         const int i = (p - yb) % AUX;
         float *b = aux + i * C::AUX_FLOATS;
         bar_arrive_expect_tx(bars + R + i, C::AUX_TX);
-        tma_load_3d(b, pmap, x0, z0, p, bars + R + i);
-        tma_load_3d(b + C::TILE_FLOATS, amap, x0, z0, p, bars + R + i);
-        tma_load_3d(b + 2 * C::TILE_FLOATS, wmap, x0 - HX, z0 - O, p, bars + R + i);
+        tma_load_3d(b, pmap, x0, z0, ys + p, bars + R + i);
+        tma_load_3d(b + C::TILE_FLOATS, amap, x0, z0, p, bars + R + i);  // shared by the shots
+        tma_load_3d(b + 2 * C::TILE_FLOATS, wmap, x0 - HX, z0 - O, ys + p, bars + R + i);
     };
 
     if (threadIdx.x == 0) {
@@ -261,7 +278,7 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     const float wz = c_wa[O - 1][lz];
     const int off = (rw + O) * TXP + HX + O * xl;  // offset of the thread's first node in the window
     const int toff = rw * TX + O * xl;             // in-tile offset (aux tiles, y-ring slots)
-    float *dst_col = a.prev + (int64_t)xb + (int64_t)z * t.nxp;
+    float *dst_col = a.prev + (MULTI ? (int64_t)shot * t.shot_stride : 0) + (int64_t)xb + (int64_t)z * t.nxp;
     const int64_t plane_stride = t.nxp * t.nz;
 
     bool ok = true;
@@ -400,13 +417,16 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
         return;
     }
     if (a.nrec > 0) {
-        const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        const int cta = bx + t.grid[0] * (bz + t.grid[1] * chunk);  // tile and chunk
         const int r0 = a.rec_off[cta], r1 = a.rec_off[cta + 1];
         if (r0 < r1) {  // uniform over the CTA; its new values are visible after the last barrier
             const int step = a.ctr[1];
+            const float *lvl = a.prev + (MULTI ? (int64_t)shot * t.shot_stride : 0);
             for (int r = r0 + threadIdx.x; r < r1; r += C::THREADS) {
                 const int j = a.rec_idx[r];
-                a.traces[(int64_t)step * a.nrec + a.rec_perm[j]] = a.prev[a.rec_node[j]];
+                // traces [step][receiver][shot]
+                const int64_t k = (int64_t)step * a.nrec + a.rec_perm[j];
+                a.traces[MULTI ? k * t.nshot + shot : k] = lvl[a.rec_node[j]];
             }
         }
     }
@@ -448,7 +468,7 @@ template <int O>
 int blocks_per_sm_of()
 {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stencil<O, true, STENCIL_PLAIN, true>, Cfg<O>::THREADS,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stencil<O, true, STENCIL_PLAIN, true, false>, Cfg<O>::THREADS,
                                                       Cfg<O>::SMEM) != cudaSuccess) {
         cudaGetLastError();
         n = 0;
@@ -467,26 +487,37 @@ int blocks_per_sm(int order)
     }
 }
 
-template <int O, bool SPONGE, int MODE, bool DIRECT>
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI>
 void launch_om(const dim3 &grid, const LevelMaps &cm, const LevelMaps &pm, const StencilTables &t,
                const StencilArgs &a, cudaStream_t s)
 {
-    k_stencil<O, SPONGE, MODE, DIRECT>
+    k_stencil<O, SPONGE, MODE, DIRECT, MULTI>
         <<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.tile, cm.win, pm.tile, t.amap, t, a);
 }
 
 template <int O, bool DIRECT>
 cudaError_t launch_of(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, int mode, cudaStream_t s)
 {
-    const dim3 grid(t.grid[0], t.grid[1], t.grid[2]);
     const LevelMaps &cm = t.lv[ci], &pm = t.lv[1 - ci];
+    if (t.nshot > 1) {
+        // many shots: plain steps in the direct form
+        if constexpr (DIRECT) {
+            if (mode != STENCIL_PLAIN) return cudaErrorInvalidValue;
+            const dim3 grid((unsigned)((int64_t)t.grid[0] * t.grid[1] * t.nshot), (unsigned)t.grid[2]);
+            if (sponge) launch_om<O, true, STENCIL_PLAIN, true, true>(grid, cm, pm, t, a, s);
+            else launch_om<O, false, STENCIL_PLAIN, true, true>(grid, cm, pm, t, a, s);
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
+    }
+    const dim3 grid(t.grid[0], t.grid[1], t.grid[2]);
     switch (mode * 2 + (sponge ? 1 : 0)) {
-    case 0: launch_om<O, false, STENCIL_PLAIN, DIRECT>(grid, cm, pm, t, a, s); break;
-    case 1: launch_om<O, true, STENCIL_PLAIN, DIRECT>(grid, cm, pm, t, a, s); break;
-    case 2: launch_om<O, false, STENCIL_RECORD_KP, DIRECT>(grid, cm, pm, t, a, s); break;
-    case 3: launch_om<O, true, STENCIL_RECORD_KP, DIRECT>(grid, cm, pm, t, a, s); break;
-    case 4: launch_om<O, false, STENCIL_GRADIENT, DIRECT>(grid, cm, pm, t, a, s); break;
-    case 5: launch_om<O, true, STENCIL_GRADIENT, DIRECT>(grid, cm, pm, t, a, s); break;
+    case 0: launch_om<O, false, STENCIL_PLAIN, DIRECT, false>(grid, cm, pm, t, a, s); break;
+    case 1: launch_om<O, true, STENCIL_PLAIN, DIRECT, false>(grid, cm, pm, t, a, s); break;
+    case 2: launch_om<O, false, STENCIL_RECORD_KP, DIRECT, false>(grid, cm, pm, t, a, s); break;
+    case 3: launch_om<O, true, STENCIL_RECORD_KP, DIRECT, false>(grid, cm, pm, t, a, s); break;
+    case 4: launch_om<O, false, STENCIL_GRADIENT, DIRECT, false>(grid, cm, pm, t, a, s); break;
+    case 5: launch_om<O, true, STENCIL_GRADIENT, DIRECT, false>(grid, cm, pm, t, a, s); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -499,11 +530,11 @@ cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, int ci, bool 
     return direct ? launch_of<O, true>(t, a, ci, sponge, mode, s) : launch_of<O, false>(t, a, ci, sponge, mode, s);
 }
 
-template <int O, bool SPONGE, int MODE, bool DIRECT>
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI = false>
 cudaError_t setup_om()
 {
-    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE, DIRECT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)Cfg<O>::SMEM);
+    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE, DIRECT, MULTI>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<O>::SMEM);
 }
 
 template <int O, bool DIRECT>
@@ -522,7 +553,10 @@ template <int O>
 cudaError_t setup_o()
 {
     cudaError_t e = setup_of<O, true>();
-    return e != cudaSuccess ? e : setup_of<O, false>();
+    if (e == cudaSuccess) e = setup_of<O, false>();
+    if (e == cudaSuccess) e = setup_om<O, true, STENCIL_PLAIN, true, true>();
+    if (e == cudaSuccess) e = setup_om<O, false, STENCIL_PLAIN, true, true>();
+    return e;
 }
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -542,12 +576,13 @@ EncodeTiled encoder()
     return fn;
 }
 
-// 3-D map over the device layout (nxp, nz, ny) of float buffer `base` with box (bx, bz, 1).
-bool make_map(CUtensorMap &m, const float *base, const StencilTables &t, int bx, int bz)
+// 3-D map over the device layout (nxp, nz, planes) of float buffer `base` with box (bx, bz, 1);
+// planes = ny, or ny * nshot for levels that stack the shots along y.
+bool make_map(CUtensorMap &m, const float *base, const StencilTables &t, int bx, int bz, int64_t planes)
 {
     EncodeTiled enc = encoder();
     if (!enc) return false;
-    const cuuint64_t dims[3] = {(cuuint64_t)t.nxp, (cuuint64_t)t.nz, (cuuint64_t)t.ny};
+    const cuuint64_t dims[3] = {(cuuint64_t)t.nxp, (cuuint64_t)t.nz, (cuuint64_t)planes};
     const cuuint64_t strides[2] = {(cuuint64_t)t.nxp * 4, (cuuint64_t)t.nxp * t.nz * 4};
     const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)bz, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
@@ -558,11 +593,14 @@ bool make_map(CUtensorMap &m, const float *base, const StencilTables &t, int bx,
 
 }  // namespace
 
-int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, StencilTables **out)
+int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int nshot, StencilTables **out)
 {
+    if (nshot < 1) return (int)cudaErrorInvalidValue;
     StencilTables *t = new StencilTables();
     t->order = b.order;
     t->nx = b.nx; t->nxp = b.nxp; t->ny = b.ny; t->nz = b.nz;
+    t->nshot = nshot;
+    t->shot_stride = b.nxp * b.nz * b.ny;
     for (int d = 0; d < 3; d++) t->g[d] = (float)geo.g[d];
     for (int l = 0; l < b.order; l++) t->wa[l] = (float)(l == 0 ? g.w[0] + g.w[b.order] : g.w[l]);
     int threads = 256;
@@ -578,7 +616,7 @@ int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, Stenc
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     per_sm = blocks_per_sm(b.order);  // kernel attributes are set up with the solver
     if (per_sm <= 0) per_sm = std::max(1, std::min(2048 / threads, smem_sm / (int)(t->smem + 1024)));
-    const int64_t cols = (int64_t)t->grid[0] * t->grid[1];
+    const int64_t cols = (int64_t)t->grid[0] * t->grid[1] * nshot;
     const int64_t resident = (int64_t)sms * per_sm;
     double best = 1e300;
     int best_c = 1;
@@ -600,11 +638,11 @@ int stencil_bind(StencilTables &t, const float *p0, const float *p1, const float
     const int txp = t.tile_x + 2 * t.halo_x;
     const float *ps[2] = {p0, p1};
     for (int i = 0; i < 2; i++) {
-        if (!make_map(t.lv[i].win, ps[i], t, txp, t.tile_z + 2 * t.order) ||
-            !make_map(t.lv[i].tile, ps[i], t, t.tile_x, t.tile_z))
+        if (!make_map(t.lv[i].win, ps[i], t, txp, t.tile_z + 2 * t.order, t.ny * t.nshot) ||
+            !make_map(t.lv[i].tile, ps[i], t, t.tile_x, t.tile_z, t.ny * t.nshot))
             return (int)cudaErrorInvalidValue;
     }
-    if (!make_map(t.amap, a, t, t.tile_x, t.tile_z)) return (int)cudaErrorInvalidValue;
+    if (!make_map(t.amap, a, t, t.tile_x, t.tile_z, t.ny)) return (int)cudaErrorInvalidValue;
     t.bound[0] = p0; t.bound[1] = p1; t.bound[2] = a;
     return 0;
 }

@@ -31,7 +31,9 @@ struct StencilTables {
     float g[3] = {0, 0, 0};   // g_d = |detJ| / J_dd^2 for x (xi1), z (xi2), y (xi3)
     float wa[6] = {0};        // assembled weight by local index: wa[0] = 2 w_0, wa[l] = w_l
     int tile_x = 0, tile_z = 0, halo_x = 0;
-    int grid[3] = {0, 0, 0};  // CTAs along x, z, y
+    int grid[3] = {0, 0, 0};  // tiles along x, z and y-chunks (launch: x * z * nshot CTAs by chunks)
+    int nshot = 1;            // shots stacked along y in the levels (many-shot form)
+    int64_t shot_stride = 0;  // floats per shot field: nxp * nz * ny
     int ychunk = 0;           // planes per CTA
     size_t smem = 0;          // dynamic shared memory per CTA
     LevelMaps lv[2];          // per pressure buffer
@@ -66,7 +68,9 @@ struct StencilArgs {
 enum StencilMode { STENCIL_PLAIN = 0, STENCIL_RECORD_KP = 1, STENCIL_GRADIENT = 2 };
 
 // Tables and tiling for a box (no device buffers yet).  Returns 0 or a cudaError_t.
-int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, StencilTables **out);
+// nshot > 1: the many-shot form, levels holding nshot fields one after another (traces
+// [step][receiver][shot]); dt^2/M and the sponge are shared.
+int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int nshot, StencilTables **out);
 // Describe the solver's two pressure buffers and its dt^2/M buffer with tensor maps.
 int stencil_bind(StencilTables &t, const float *p0, const float *p1, const float *a);
 // Group node-sorted receivers (device-layout indices) by owning CTA (device CSR in t).
