@@ -36,11 +36,11 @@ namespace {
 #ifndef SEM_STENCIL_LOOKAHEAD
 #define SEM_STENCIL_LOOKAHEAD 1
 #endif
-#ifndef SEM_STENCIL_ROWS
-#define SEM_STENCIL_ROWS 8  // warps per CTA
+#ifndef SEM_STENCIL_NG
+#define SEM_STENCIL_NG 2  // row groups per thread where the order allows it
 #endif
 #ifndef SEM_STENCIL_RW
-#define SEM_STENCIL_RW 2  // rows per warp where the order allows it
+#define SEM_STENCIL_RW 2  // rows per warp instruction where the order allows it
 #endif
 constexpr int kLook = SEM_STENCIL_LOOKAHEAD;  // planes of lookahead
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
@@ -50,13 +50,19 @@ __constant__ float c_wa[kMaxOrder][kMaxOrder];  // assembled weights by local in
 
 template <int O>
 struct Cfg {
-    static constexpr int WARPS = O == 5 ? 8 : SEM_STENCIL_ROWS;
-    // A warp's lanes split into RW groups on rows O apart, so that the z-local index stays
-    // warp-uniform (needs WARPS a multiple of O); narrower tiles waste fewer lanes on the last
-    // x-tile of a row (801 nodes: 13 tiles of 64 against 7 of 128).
-    static constexpr int RW = WARPS % O == 0 ? SEM_STENCIL_RW : 1;
+    // Orders 1, 2, 4 (o divides the warp count): a warp's lanes split into RW sets on rows o
+    // apart, and each thread owns NG row groups a further o*RW rows apart, all with the same
+    // z-local index (warp-uniform coefficients).  Narrow tiles waste fewer lanes on the last
+    // x-tile of a row (801 nodes: 13 tiles of 64 against 7 of 128); the groups share one
+    // thread's per-plane bookkeeping (waits, slot selection, coefficient dispatch, sponge).
+    // Orders 3 and 5: one row per warp, 8 warps.
+    static constexpr bool SPLIT = O == 1 || O == 2 || O == 4;
+    static constexpr int NG = SPLIT ? SEM_STENCIL_NG : 1;  // row groups per thread
+    static constexpr int WARPS = SPLIT ? 8 / NG : 8;
+    static constexpr int RW = SPLIT ? SEM_STENCIL_RW : 1;
     static constexpr int LANES = 32 / RW;               // lanes per row
-    static constexpr int TZ = WARPS * RW;               // rows per CTA
+    static constexpr int GR = O * RW;                   // rows between a thread's groups
+    static constexpr int TZ = WARPS * RW * NG;          // rows per CTA
     static constexpr int THREADS = 32 * WARPS;
     static constexpr int TX = LANES * O;                // nodes along x per CTA
     static constexpr int HX = O <= 4 ? 4 : 8;           // x halo, a multiple of 4 floats
@@ -112,71 +118,83 @@ __device__ __forceinline__ void load_o_lim(const float *p, float (&v)[O], int li
     }
 }
 
-template <int O>
-struct VecO {
-    float v[O];
+template <int O, int NG>
+struct VecG {
+    float v[NG][O];
 };
 
-// Axis term along a direction whose local index LOC is uniform over the thread's O nodes:
-// direct form r[j] = sum_d T[LOC][d] row(d)[j] (diagonal included), difference form
-// r[j] = sum_{d!=0} T[LOC][d] (row(d)[j] - c[j]).  row(d) returns the pointer to the O values
-// at offset d along the axis.
-template <int O, int LOC, bool DIRECT, class RowFn>
-__device__ __forceinline__ VecO<O> axis_uniform(const float (&c)[O], const RowFn &row)
+// Axis term along a direction whose local index LOC is uniform over the thread's NG groups of O
+// nodes: direct form r[g][j] = sum_d T[LOC][d] row_g(d)[j] (diagonal included), difference form
+// r[g][j] = sum_{d!=0} T[LOC][d] (row_g(d)[j] - c[g][j]).  row(d) returns the pointer to group
+// 0's O values at offset d along the axis; group g's lie g*GS floats further.
+template <int O, int NG, int GS, int LOC, bool DIRECT, class RowFn>
+__device__ __forceinline__ VecG<O, NG> axis_uniform(const float (&c)[NG][O], const RowFn &row)
 {
-    VecO<O> r;
+    VecG<O, NG> r;
     if constexpr (DIRECT) {
         // the coefficients are constant-bank operands of scalar fmas
 #pragma unroll
-        for (int j = 0; j < O; j++) r.v[j] = c_T[O - 1][LOC * (2 * O + 1) + O] * c[j];
+        for (int g = 0; g < NG; g++)
+#pragma unroll
+            for (int j = 0; j < O; j++) r.v[g][j] = c_T[O - 1][LOC * (2 * O + 1) + O] * c[g][j];
 #pragma unroll
         for (int d = dlo(O, LOC); d <= dhi(O, LOC); d++) {
             if (d == 0) continue;
-            float v[O];
-            load_o<O>(row(d), v);
+            const float *p = row(d);
 #pragma unroll
-            for (int j = 0; j < O; j++) r.v[j] = fmaf(c_T[O - 1][LOC * (2 * O + 1) + d + O], v[j], r.v[j]);
+            for (int g = 0; g < NG; g++) {
+                float v[O];
+                load_o<O>(p + g * GS, v);
+#pragma unroll
+                for (int j = 0; j < O; j++) r.v[g][j] = fmaf(c_T[O - 1][LOC * (2 * O + 1) + d + O], v[j], r.v[g][j]);
+            }
         }
     } else {
 #pragma unroll
-        for (int j = 0; j < O; j++) r.v[j] = 0.f;
+        for (int g = 0; g < NG; g++)
+#pragma unroll
+            for (int j = 0; j < O; j++) r.v[g][j] = 0.f;
 #pragma unroll
         for (int d = dlo(O, LOC); d <= dhi(O, LOC); d++) {
             if (d == 0) continue;
-            float v[O];
-            load_o<O>(row(d), v);
+            const float *p = row(d);
             const float t = c_T[O - 1][LOC * (2 * O + 1) + d + O];
-            if constexpr (O % 2 == 0) {
-                // the coefficient is shared by the thread's nodes: pairs of nodes in packed f32x2
-                // (each half rounds as the scalar sub and fma would)
 #pragma unroll
-                for (int j = 0; j < O; j += 2) {
-                    const float2 acc = fma2(make_float2(t, t),
-                                            sub2(make_float2(v[j], v[j + 1]), make_float2(c[j], c[j + 1])),
-                                            make_float2(r.v[j], r.v[j + 1]));
-                    r.v[j] = acc.x;
-                    r.v[j + 1] = acc.y;
+            for (int g = 0; g < NG; g++) {
+                float v[O];
+                load_o<O>(p + g * GS, v);
+                if constexpr (O % 2 == 0) {
+                    // the coefficient is shared by the thread's nodes: pairs of nodes in packed
+                    // f32x2 (each half rounds as the scalar sub and fma would)
+#pragma unroll
+                    for (int j = 0; j < O; j += 2) {
+                        const float2 acc = fma2(make_float2(t, t),
+                                                sub2(make_float2(v[j], v[j + 1]), make_float2(c[g][j], c[g][j + 1])),
+                                                make_float2(r.v[g][j], r.v[g][j + 1]));
+                        r.v[g][j] = acc.x;
+                        r.v[g][j + 1] = acc.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < O; j++) r.v[g][j] = fmaf(t, v[j] - c[g][j], r.v[g][j]);
                 }
-            } else {
-#pragma unroll
-                for (int j = 0; j < O; j++) r.v[j] = fmaf(t, v[j] - c[j], r.v[j]);
             }
         }
     }
     return r;
 }
 
-template <int O, bool DIRECT, class RowFn>
-__device__ __forceinline__ VecO<O> axis_dispatch(int loc, const float (&c)[O], const RowFn &row)
+template <int O, int NG, int GS, bool DIRECT, class RowFn>
+__device__ __forceinline__ VecG<O, NG> axis_dispatch(int loc, const float (&c)[NG][O], const RowFn &row)
 {
     switch (loc) {
-    case 0: return axis_uniform<O, 0, DIRECT>(c, row);
-    case 1: if constexpr (O > 1) return axis_uniform<O, 1, DIRECT>(c, row);
-    case 2: if constexpr (O > 2) return axis_uniform<O, 2, DIRECT>(c, row);
-    case 3: if constexpr (O > 3) return axis_uniform<O, 3, DIRECT>(c, row);
-    default: if constexpr (O > 4) return axis_uniform<O, 4, DIRECT>(c, row);
+    case 0: return axis_uniform<O, NG, GS, 0, DIRECT>(c, row);
+    case 1: if constexpr (O > 1) return axis_uniform<O, NG, GS, 1, DIRECT>(c, row);
+    case 2: if constexpr (O > 2) return axis_uniform<O, NG, GS, 2, DIRECT>(c, row);
+    case 3: if constexpr (O > 3) return axis_uniform<O, NG, GS, 3, DIRECT>(c, row);
+    default: if constexpr (O > 4) return axis_uniform<O, NG, GS, 4, DIRECT>(c, row);
     }
-    return axis_uniform<O, 0, DIRECT>(c, row);  // not reached: loc < O
+    return axis_uniform<O, NG, GS, 0, DIRECT>(c, row);  // not reached: loc < O
 }
 
 // z-neighbour rows: window rows are contiguous over the tile and its z halo.
@@ -262,24 +280,36 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
         for (int p = yb; p <= min(yb + kLook - 1, ye - 1); p++) issue_aux(p);
     }
 
-    // per-thread constants
-    // tile row and x group of the thread: rows of one warp share z mod O
+    // per-thread constants.  Tile row of the thread's group 0 and its x position: the rows of
+    // one warp (and of all groups of a thread) share z mod O; group g lies g*GR rows further.
+    constexpr int NG = C::NG, GR = C::GR;
     const int xl = l % C::LANES;
-    const int rw = C::RW == 1 ? w : (w / O) * (O * C::RW) + w % O + (l / C::LANES) * O;
+    const int rw = C::RW == 1 && NG == 1 ? w : (w / O) * (O * C::RW * NG) + w % O + (l / C::LANES) * O;
     const int z = z0 + rw;
-    const bool row_ok = z < nz;
-    const bool zin = z > 0 && z < nz - 1;
     const int lz = z % O;
     const int xb = x0 + O * xl;  // first node of the thread
     float sxv[O];
 #pragma unroll
     for (int j = 0; j < O; j++) sxv[j] = (SPONGE && xb + j < nx) ? __ldg(a.sx + xb + j) : 1.f;
-    const float szv = (SPONGE && row_ok) ? __ldg(a.sz + z) : 1.f;
+    bool row_ok[NG], zin[NG];
+    bool zin_all = true;
+    float sxz[NG][O];  // (sx*sz) of the thread's nodes; the node factor is (sx*sz)*sy
+#pragma unroll
+    for (int g = 0; g < NG; g++) {
+        const int zg = z + g * GR;
+        row_ok[g] = zg < nz;
+        zin[g] = zg > 0 && zg < nz - 1;
+        zin_all = zin_all && zin[g];
+        const float szv = (SPONGE && row_ok[g]) ? __ldg(a.sz + zg) : 1.f;
+#pragma unroll
+        for (int j = 0; j < O; j++) sxz[g][j] = sxv[j] * szv;
+    }
     const float wz = c_wa[O - 1][lz];
     const int off = (rw + O) * TXP + HX + O * xl;  // offset of the thread's first node in the window
     const int toff = rw * TX + O * xl;             // in-tile offset (aux tiles, y-ring slots)
     float *dst_col = a.prev + (MULTI ? (int64_t)shot * t.shot_stride : 0) + (int64_t)xb + (int64_t)z * t.nxp;
     const int64_t plane_stride = t.nxp * t.nz;
+    const int64_t group_stride = (int64_t)GR * t.nxp;
 
     bool ok = true;
     for (int p = yb - O; p < yb + O; p++) {
@@ -289,12 +319,10 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     if (!ok) atomicExch(a.status, 1);
     bool aborted = __syncthreads_or(!ok) != 0;
 
-    // all O nodes of the thread strictly inside the mesh along x: no per-node checks on the
+    // all nodes of the thread strictly inside the mesh along x and z: no per-node checks on the
     // common path
     const bool xall = xb > 0 && xb + O < nx;
-    float sxz[O];  // (sx*sz) of the thread's nodes; the node factor is (sx*sz)*sy
-#pragma unroll
-    for (int j = 0; j < O; j++) sxz[j] = sxv[j] * szv;
+    const bool inner = xall && zin_all;
 
     int rs = O;         // ring slot of plane y
     int ws = 2 * O;     // ring slot of plane y+O, the one waited for (2O < R), and its phase
@@ -310,94 +338,118 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
         ok = bar_wait(bars + ws, wph, kWaitLimitNs);
         ok &= bar_wait(bars + R + as, aph, kWaitLimitNs);
         if (!ok) atomicExch(a.status, 1);
-        if (row_ok) {
+        {
+            // rows past the mesh read zero-filled shared memory; only their stores are skipped
             const float *cur = aux + as * C::AUX_FLOATS + 2 * C::TILE_FLOATS + off;  // window
             const float *tq = aux + as * C::AUX_FLOATS + toff;
-            float c[O], left[O], q[O], am[O];
-            load_o<O>(cur, c);
-            load_o<O>(cur - O, left);
-            const float right = cur[O];
-            load_o<O>(tq, q);
-            load_o<O>(tq + C::TILE_FLOATS, am);
+            float c[NG][O], left[NG][O], right[NG], q[NG][O], am[NG][O];
+#pragma unroll
+            for (int g = 0; g < NG; g++) {
+                load_o<O>(cur + g * GR * TXP, c[g]);
+                load_o<O>(cur + g * GR * TXP - O, left[g]);
+                right[g] = cur[g * GR * TXP + O];
+                load_o<O>(tq + g * GR * TX, q[g]);
+                load_o<O>(tq + g * GR * TX + C::TILE_FLOATS, am[g]);
+            }
 
             // x: local index j is compile-time
-            float ax[O];
+            float ax[NG][O];
 #pragma unroll
-            for (int j = 0; j < O; j++) {
-                float acc = DIRECT ? c_T[O - 1][j * (2 * O + 1) + O] * c[j] : 0.f;
-                // constant trip count, so that the loop unrolls together with j and every index
-                // below is a constant (a j-dependent range left it rolled, with the arrays in memory)
+            for (int g = 0; g < NG; g++)
 #pragma unroll
-                for (int d = -O; d <= O; d++) {
-                    if (d == 0 || d < dlo(O, j) || d > dhi(O, j)) continue;
-                    const int m = j + d;  // offset from the thread's first node, in [-O, O]
-                    const float v = m < 0 ? left[m + O] : (m < O ? c[m] : right);
-                    acc = fmaf(c_T[O - 1][j * (2 * O + 1) + d + O], DIRECT ? v : v - c[j], acc);
+                for (int j = 0; j < O; j++) {
+                    float acc = DIRECT ? c_T[O - 1][j * (2 * O + 1) + O] * c[g][j] : 0.f;
+                    // constant trip count, so that the loop unrolls together with j and every
+                    // index below is a constant (a j-dependent range left it rolled, with the
+                    // arrays in memory)
+#pragma unroll
+                    for (int d = -O; d <= O; d++) {
+                        if (d == 0 || d < dlo(O, j) || d > dhi(O, j)) continue;
+                        const int m = j + d;  // offset from the thread's first node, in [-O, O]
+                        const float v = m < 0 ? left[g][m + O] : (m < O ? c[g][m] : right[g]);
+                        acc = fmaf(c_T[O - 1][j * (2 * O + 1) + d + O], DIRECT ? v : v - c[g][j], acc);
+                    }
+                    ax[g][j] = acc;
                 }
-                ax[j] = acc;
-            }
-            const VecO<O> az = axis_dispatch<O, DIRECT>(lz, c, ZRows{cur, TXP});
+            const VecG<O, NG> az = axis_dispatch<O, NG, GR * TXP, DIRECT>(lz, c, ZRows{cur, TXP});
             const float *yb0 = ring + rs * C::RING_FLOATS + toff;
             const YPlanes<R, C::RING_FLOATS> yrows{yb0, yb0 + R * C::RING_FLOATS, yb0 - R * C::RING_FLOATS, rs};
-            const VecO<O> ay = axis_dispatch<O, DIRECT>(ly, c, yrows);
+            const VecG<O, NG> ay = axis_dispatch<O, NG, GR * TX, DIRECT>(ly, c, yrows);
 
             const bool yin = y > 0 && y < ny - 1;
             const float wy = c_wa[O - 1][ly];
             const float syv = SPONGE ? __ldg(a.sy + y) : 1.f;
             const float gx = t.g[0] * (wz * wy), gzy = t.g[1] * wy, gyz = t.g[2] * wz;
-            float out[O], kp[O];
-            if (MODE == STENCIL_GRADIENT)
-                load_o_lim<O>(a.kp + (dst_col - a.prev) + (int64_t)y * plane_stride, kp, (int)t.nxp - xb);
-            float sv[O], qdv[O];
+            float *dst = dst_col + (int64_t)y * plane_stride;
+            float out[NG][O], kp[NG][O], sv[NG][O], qdv[NG][O];
 #pragma unroll
-            for (int j = 0; j < O; j++) {
-                const float wxj = c_wa[O - 1][j];
-                sv[j] = SPONGE ? sxz[j] * syv : 1.f;
-                qdv[j] = SPONGE ? sv[j] * q[j] : q[j];
-                // K.p at the node: g1 Wz Wy A_x + Wx (g2 Wy A_z + g3 Wz A_y)
-                const float yv = fmaf(wxj, fmaf(gyz, ay.v[j], gzy * az.v[j]), gx * ax[j]);
-                out[j] = (2.f * c[j] - qdv[j]) - am[j] * yv;
-                if (MODE == STENCIL_RECORD_KP) kp[j] = yv;
+            for (int g = 0; g < NG; g++) {
+                if (MODE == STENCIL_GRADIENT) {
+                    if (row_ok[g])
+                        load_o_lim<O>(a.kp + (dst - a.prev) + g * group_stride, kp[g], (int)t.nxp - xb);
+                    else
+#pragma unroll
+                        for (int j = 0; j < O; j++) kp[g][j] = 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < O; j++) {
+                    const float wxj = c_wa[O - 1][j];
+                    sv[g][j] = SPONGE ? sxz[g][j] * syv : 1.f;
+                    qdv[g][j] = SPONGE ? sv[g][j] * q[g][j] : q[g][j];
+                    // K.p at the node: g1 Wz Wy A_x + Wx (g2 Wy A_z + g3 Wz A_y)
+                    const float yv = fmaf(wxj, fmaf(gyz, ay.v[g][j], gzy * az.v[g][j]), gx * ax[g][j]);
+                    out[g][j] = (2.f * c[g][j] - qdv[g][j]) - am[g][j] * yv;
+                    if (MODE == STENCIL_RECORD_KP) kp[g][j] = yv;
+                }
             }
-            if (!(xall && zin && yin)) {
+            if (!(inner && yin)) {
                 // boundary and padding nodes: no update (the stored previous level is kept, then
                 // damped), padding columns stay zero
 #pragma unroll
-                for (int j = 0; j < O; j++) {
-                    if (!(xb + j > 0 && xb + j < nx - 1 && zin && yin)) {
-                        out[j] = qdv[j];
-                        if (MODE == STENCIL_RECORD_KP) kp[j] = 0.f;
+                for (int g = 0; g < NG; g++)
+#pragma unroll
+                    for (int j = 0; j < O; j++) {
+                        if (!(xb + j > 0 && xb + j < nx - 1 && zin[g] && yin)) {
+                            out[g][j] = qdv[g][j];
+                            if (MODE == STENCIL_RECORD_KP) kp[g][j] = 0.f;
+                        }
                     }
+            }
+#pragma unroll
+            for (int g = 0; g < NG; g++)
+#pragma unroll
+                for (int j = 0; j < O; j++) {
+                    if (SPONGE) out[g][j] = sv[g][j] * out[g][j];
+                    if (!xall && xb + j >= nx) out[g][j] = 0.f;
                 }
-            }
 #pragma unroll
-            for (int j = 0; j < O; j++) {
-                if (SPONGE) out[j] = sv[j] * out[j];
-                if (!xall && xb + j >= nx) out[j] = 0.f;
-            }
-            float *dst = dst_col + (int64_t)y * plane_stride;
-            if (MODE != STENCIL_PLAIN) {
-                // side buffers: same device layout as the levels; padding columns stay untouched
-                const int64_t off = dst - a.prev;
-                if (MODE == STENCIL_GRADIENT) {
-                    float g[O];
-                    load_o_lim<O>(a.grad + off, g, (int)t.nxp - xb);
+            for (int g = 0; g < NG; g++) {
+                if (!row_ok[g]) continue;
+                float *dg = dst + g * group_stride;
+                if (MODE != STENCIL_PLAIN) {
+                    // side buffers: same device layout as the levels; padding columns stay untouched
+                    const int64_t so = dg - a.prev;
+                    if (MODE == STENCIL_GRADIENT) {
+                        float gr[O];
+                        load_o_lim<O>(a.grad + so, gr, (int)t.nxp - xb);
 #pragma unroll
-                    for (int j = 0; j < O; j++) kp[j] = fmaf(c[j], kp[j], g[j]);
+                        for (int j = 0; j < O; j++) kp[g][j] = fmaf(c[g][j], kp[g][j], gr[j]);
+                    }
+                    float *side = (MODE == STENCIL_GRADIENT ? a.grad : a.kp) + so;
+#pragma unroll
+                    for (int j = 0; j < O; j++)
+                        if (xb + j < nx) side[j] = kp[g][j];
                 }
-                float *side = (MODE == STENCIL_GRADIENT ? a.grad : a.kp) + off;
+                if constexpr (O == 4) {
+                    if (xb + 4 <= t.nxp)
+                        *reinterpret_cast<float4 *>(dg) = make_float4(out[g][0], out[g][1], out[g][2], out[g][3]);
+                } else if constexpr (O == 2) {
+                    if (xb + 2 <= t.nxp) *reinterpret_cast<float2 *>(dg) = make_float2(out[g][0], out[g][1]);
+                } else {
 #pragma unroll
-                for (int j = 0; j < O; j++)
-                    if (xb + j < nx) side[j] = kp[j];
-            }
-            if constexpr (O == 4) {
-                if (xb + 4 <= t.nxp) *reinterpret_cast<float4 *>(dst) = make_float4(out[0], out[1], out[2], out[3]);
-            } else if constexpr (O == 2) {
-                if (xb + 2 <= t.nxp) *reinterpret_cast<float2 *>(dst) = make_float2(out[0], out[1]);
-            } else {
-#pragma unroll
-                for (int j = 0; j < O; j++)
-                    if (xb + j < t.nxp) dst[j] = out[j];
+                    for (int j = 0; j < O; j++)
+                        if (xb + j < t.nxp) dg[j] = out[g][j];
+                }
             }
         }
         aborted = __syncthreads_or(!ok) != 0;
