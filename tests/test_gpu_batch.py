@@ -1,7 +1,8 @@
-"""Batched form (many shots on one mesh, sem_batch_*): every shot of a batch must match the plain
-solver run of that shot alone (the plain solver is itself pinned to the reference), traces and
-pressure, and autotuning must not change the state.  Both paths evaluate the same assembled
-operator with different summation orders; tolerance relative L2 <= 5e-6 after 60 steps."""
+"""Batched form (many shots on one mesh, sem_batch_*): every shot of a batch must give the same
+bits as the plain solver run of that shot alone (the plain solver is itself pinned to the
+reference): the batch steps the shot-stacked levels with the plain stencil pass's own
+arithmetic.  Traces and both pressure levels are compared, for batch sizes that are and are not
+multiples of 32, and autotuning must not change the state."""
 import numpy as np
 import pytest
 
@@ -42,9 +43,9 @@ def test_batch_matches_plain_solver_per_shot(semgb_lib, cuda_device, order, n_sh
         p.set_source_points(wl.src_xyz[s:s + 1], wav[s:s + 1])
         p.set_receivers(wl.rec_xyz)
         p.step(wl.nsteps)
-        assert rel_l2(tr[:, :, s], p.traces()) <= 5e-6
-        assert rel_l2(b.pressure(s), p.pressure()) <= 5e-6
-        assert rel_l2(b.pressure(s, semgb.LEVEL_PREVIOUS), p.pressure(semgb.LEVEL_PREVIOUS)) <= 5e-6
+        assert np.array_equal(tr[:, :, s], p.traces())
+        assert np.array_equal(b.pressure(s), p.pressure())
+        assert np.array_equal(b.pressure(s, semgb.LEVEL_PREVIOUS), p.pressure(semgb.LEVEL_PREVIOUS))
         p.close()
 
 
@@ -66,5 +67,5 @@ def test_batch_autotune_keeps_state(semgb_lib, cuda_device):
         b.step(40)
         res.append((b.traces(), b.pressure(7)))
         b.close()
-    assert rel_l2(res[1][0], res[0][0]) <= 5e-6
-    assert rel_l2(res[1][1], res[0][1]) <= 5e-6
+    assert np.array_equal(res[1][0], res[0][0])
+    assert np.array_equal(res[1][1], res[0][1])
