@@ -50,6 +50,9 @@ int solver_set_raw_sources(sem_solver *s, int n_src, const int64_t *nodes, const
     s->nsamples = n_samples;
     s->src_node.assign(nodes, nodes + n_src);
     s->src_coef.assign(coef, coef + n_src);
+    std::vector<int64_t> sorted(nodes, nodes + n_src);
+    std::sort(sorted.begin(), sorted.end());
+    s->src_distinct = std::adjacent_find(sorted.begin(), sorted.end()) == sorted.end();
     if (n_src > 0) {
         CUDA_TRY(dalloc(&s->d_src_node, n_src));
         CUDA_TRY(dalloc(&s->d_src_coef, n_src));
@@ -582,7 +585,7 @@ cudaError_t solver_enqueue_step(sem_solver *s, int c, cudaEvent_t *ev, const Ste
     const Box &b = m->box;
     cudaError_t e;
     SourceArgs sa{s->d_p[c], s->d_src_node, s->d_src_coef, s->d_wavelet, s->nsamples > 0 ? s->nsrc : 0,
-                  s->nsamples, s->d_ctr};
+                  s->nsamples, s->d_ctr, s->src_distinct ? 1 : 0};
     if (ev) cudaEventRecord(ev[0], s->stream);
     if ((e = launch_source(sa, s->stream)) != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[1], s->stream);

@@ -50,15 +50,15 @@ __constant__ float c_wa[kMaxOrder][kMaxOrder];  // assembled weights by local in
 
 template <int O>
 struct Cfg {
-    // Orders 1, 2, 4 (o divides the warp count): a warp's lanes split into RW sets on rows o
-    // apart, and each thread owns NG row groups a further o*RW rows apart, all with the same
-    // z-local index (warp-uniform coefficients).  Narrow tiles waste fewer lanes on the last
-    // x-tile of a row (801 nodes: 13 tiles of 64 against 7 of 128); the groups share one
-    // thread's per-plane bookkeeping (waits, slot selection, coefficient dispatch, sponge).
-    // Orders 3 and 5: one row per warp, 8 warps.
-    static constexpr bool SPLIT = O == 1 || O == 2 || O == 4;
+    // Orders 1-4 (o divides the warp count: 4 warps, 3 for o = 3): a warp's lanes split into RW
+    // sets on rows o apart, and each thread owns NG row groups a further o*RW rows apart, all
+    // with the same z-local index (warp-uniform coefficients).  Narrow tiles waste fewer lanes
+    // on the last x-tile of a row (801 nodes: 13 tiles of 64 against 7 of 128; 289 nodes at
+    // o = 3: 7 of 48 against 4 of 96); the groups share one thread's per-plane bookkeeping
+    // (waits, slot selection, coefficient dispatch, sponge).  Order 5: one row per warp, 8 warps.
+    static constexpr bool SPLIT = O <= 4;
     static constexpr int NG = SPLIT ? SEM_STENCIL_NG : 1;  // row groups per thread
-    static constexpr int WARPS = SPLIT ? 8 / NG : 8;
+    static constexpr int WARPS = !SPLIT ? 8 : (O == 3 ? 3 : 8 / NG);
     static constexpr int RW = SPLIT ? SEM_STENCIL_RW : 1;
     static constexpr int LANES = 32 / RW;               // lanes per row
     static constexpr int GR = O * RW;                   // rows between a thread's groups
@@ -81,8 +81,10 @@ struct Cfg {
     static constexpr size_t SMEM = OFF_BAR + 8 * (R + AUX);
     static constexpr uint32_t RING_TX = sizeof(float) * TZ * TX;
     static constexpr uint32_t AUX_TX = sizeof(float) * (2 * TZ * TX + TZP * TXP);
-    // three CTAs per SM where shared memory allows (the register cap follows: 85 per thread)
-    static constexpr int MIN_BLOCKS = WARPS > 8 ? 1 : (SMEM <= 74 * 1024 ? 3 : 2);
+    // CTAs per SM that shared memory allows (228 KB per SM, 1 KB reserved per CTA), at most 6;
+    // the register cap follows from it
+    static constexpr int BY_SMEM = (int)(233472 / (SMEM + 1024));
+    static constexpr int MIN_BLOCKS = BY_SMEM < 1 ? 1 : (BY_SMEM > 6 ? 6 : BY_SMEM);
 };
 
 // Offsets d with a non-zero coefficient for local index l: [-o, o] for l == 0 (element face),
@@ -116,6 +118,21 @@ __device__ __forceinline__ void load_o_lim(const float *p, float (&v)[O], int li
 #pragma unroll
         for (int j = 0; j < O; j++) v[j] = j < lim ? p[j] : 0.f;
     }
+}
+
+// Stores O values at p, of which the first `lim` lie inside the row's allocation (padding
+// columns included); one vector store when all do and the width allows it.
+template <int O>
+__device__ __forceinline__ void store_o_lim(float *p, const float (&v)[O], int lim)
+{
+    if constexpr (O == 4) {
+        if (lim >= 4) { *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]); return; }
+    } else if constexpr (O == 2) {
+        if (lim >= 2) { *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]); return; }
+    }
+#pragma unroll
+    for (int j = 0; j < O; j++)
+        if (j < lim) p[j] = v[j];
 }
 
 template <int O, int NG>
@@ -335,6 +352,22 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
             issue_ring(y + O + kLook);
             issue_aux(y + kLook);
         }
+        // gradient pass: the recorded K p' and the running gradient of the thread's nodes, loaded
+        // before the waits so that their latency overlaps the plane's work
+        float kpv[NG][O], grv[NG][O];
+        if constexpr (MODE == STENCIL_GRADIENT) {
+            const int64_t so = (dst_col - a.prev) + (int64_t)y * plane_stride;
+#pragma unroll
+            for (int g = 0; g < NG; g++) {
+                if (row_ok[g]) {
+                    load_o_lim<O>(a.kp + so + g * group_stride, kpv[g], (int)t.nxp - xb);
+                    load_o_lim<O>(a.grad + so + g * group_stride, grv[g], (int)t.nxp - xb);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < O; j++) kpv[g][j] = grv[g][j] = 0.f;
+                }
+            }
+        }
         ok = bar_wait(bars + ws, wph, kWaitLimitNs);
         ok &= bar_wait(bars + R + as, aph, kWaitLimitNs);
         if (!ok) atomicExch(a.status, 1);
@@ -384,13 +417,6 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
             float out[NG][O], kp[NG][O], sv[NG][O], qdv[NG][O];
 #pragma unroll
             for (int g = 0; g < NG; g++) {
-                if (MODE == STENCIL_GRADIENT) {
-                    if (row_ok[g])
-                        load_o_lim<O>(a.kp + (dst - a.prev) + g * group_stride, kp[g], (int)t.nxp - xb);
-                    else
-#pragma unroll
-                        for (int j = 0; j < O; j++) kp[g][j] = 0.f;
-                }
 #pragma unroll
                 for (int j = 0; j < O; j++) {
                     const float wxj = c_wa[O - 1][j];
@@ -427,18 +453,13 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
                 if (!row_ok[g]) continue;
                 float *dg = dst + g * group_stride;
                 if (MODE != STENCIL_PLAIN) {
-                    // side buffers: same device layout as the levels; padding columns stay untouched
+                    // side buffers: same device layout as the levels (padding columns hold zeros:
+                    // K p' is 0 there and the gradient keeps its value)
                     const int64_t so = dg - a.prev;
-                    if (MODE == STENCIL_GRADIENT) {
-                        float gr[O];
-                        load_o_lim<O>(a.grad + so, gr, (int)t.nxp - xb);
+                    if (MODE == STENCIL_GRADIENT)
 #pragma unroll
-                        for (int j = 0; j < O; j++) kp[g][j] = fmaf(c[g][j], kp[g][j], gr[j]);
-                    }
-                    float *side = (MODE == STENCIL_GRADIENT ? a.grad : a.kp) + so;
-#pragma unroll
-                    for (int j = 0; j < O; j++)
-                        if (xb + j < nx) side[j] = kp[g][j];
+                        for (int j = 0; j < O; j++) kp[g][j] = fmaf(c[g][j], kpv[g][j], grv[g][j]);
+                    store_o_lim<O>((MODE == STENCIL_GRADIENT ? a.grad : a.kp) + so, kp[g], (int)t.nxp - xb);
                 }
                 if constexpr (O == 4) {
                     if (xb + 4 <= t.nxp)

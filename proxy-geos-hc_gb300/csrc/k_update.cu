@@ -14,15 +14,26 @@ namespace semgb {
 
 namespace {
 
+// One block.  Sources on distinct nodes are added by all threads (one addition per node, the
+// same bits as any order); otherwise one thread adds them in source order, as the reference's
+// loop does, so that sources sharing a node sum in that order.
 __global__ void k_source(const SourceArgs a)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int n = a.ctr[0];
-    if (n < a.nsamples)
-        for (int k = 0; k < a.nsrc; k++)  // in source order, as the reference's loop
-            a.cur[a.node[k]] += a.coef[k] * a.wavelet[(int64_t)k * a.nsamples + n];
-    a.ctr[1] = n;
-    a.ctr[0] = n + 1;
+    __syncthreads();  // every thread has read the step before thread 0 advances the counter
+    if (n < a.nsamples) {
+        if (a.distinct) {
+            for (int k = threadIdx.x; k < a.nsrc; k += blockDim.x)
+                a.cur[a.node[k]] += a.coef[k] * a.wavelet[(int64_t)k * a.nsamples + n];
+        } else if (threadIdx.x == 0) {
+            for (int k = 0; k < a.nsrc; k++)
+                a.cur[a.node[k]] += a.coef[k] * a.wavelet[(int64_t)k * a.nsamples + n];
+        }
+    }
+    if (threadIdx.x == 0) {
+        a.ctr[1] = n;
+        a.ctr[0] = n + 1;
+    }
 }
 
 template <bool SPONGE>
@@ -180,7 +191,7 @@ cudaError_t launch_update(const UpdateArgs &a, bool sponge, cudaStream_t s)
 
 cudaError_t launch_source(const SourceArgs &a, cudaStream_t s)
 {
-    k_source<<<1, 32, 0, s>>>(a);
+    k_source<<<1, a.distinct && a.nsrc > 32 ? 256 : 32, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -60,6 +60,7 @@ struct SourceArgs {
     const float *wavelet;  // [nsrc][nsamples]
     int nsrc, nsamples;
     int *ctr;              // ctr[0] = next step index (advanced here), ctr[1] = this step
+    int distinct;          // 1: no two sources share a node, so they may be added in parallel
 };
 
 constexpr int kUpdateThreads = 256;

@@ -30,6 +30,7 @@ struct sem_solver {
     float *d_sx = nullptr, *d_sy = nullptr, *d_sz = nullptr;
     // sources
     int nsrc = 0, nsamples = 0;
+    bool src_distinct = true;  // no two sources on one node
     int64_t *d_src_node = nullptr;
     float *d_src_coef = nullptr;
     float *d_wavelet = nullptr;
