@@ -160,23 +160,36 @@ def rollout_samples(s: Setup, net: Mlp, per_step: int = 4000, seed: int = 0, min
 
 
 def train_network(s: Setup, net: Mlp, rounds: int = 3, epochs: int = 12, per_step: int = 3000, batch: int = 2048,
-                  lr: float = 1e-3, seed: int = 0):
+                  lr: float = 1e-3, seed: int = 0, select: bool = True):
     """Teacher-forced samples first, then `rounds` rounds of samples from runs with the current
-    network, each followed by training on everything gathered so far.  Returns the per-round
-    sample counts and final losses."""
+    network, each followed by training on everything gathered so far.  With `select`, every
+    round's network is scored by its reflected energy on `s` and the best one is kept (the
+    rounds do not improve monotonically: the teacher-forced network alone reflects more than
+    the sponge, the first rollout round far less, later ones drift).  Returns the per-round
+    sample counts, final losses and scores."""
     xs, ts = [], []
     x, t = teacher_forced_samples(s, per_step, seed)
     xs.append(x)
     ts.append(np.clip(t, -1.0, 1.0))
     log = []
+    best = None  # (energy, params, round)
     for r in range(rounds + 1):
         X, Tt = np.concatenate(xs), np.concatenate(ts)
         losses = net.train(X, Tt, epochs=epochs, batch=batch, lr=lr, seed=seed + r)
-        log.append({"round": r, "samples": int(len(X)), "loss": float(losses[-1]) if len(losses) else None})
+        entry = {"round": r, "samples": int(len(X)), "loss": float(losses[-1]) if len(losses) else None}
+        if select:
+            e, _ = reflected_energy(s, net)
+            entry["reflected_energy"] = e
+            if best is None or e < best[0]:
+                best = (e, net.params.copy(), r)
+        log.append(entry)
         if r < rounds:
             x, t = rollout_samples(s, net, per_step, seed + 100 + r)
             xs.append(x)
             ts.append(t)
+    if select and best is not None:
+        net.params = best[1]
+        log.append({"selected_round": best[2], "reflected_energy": best[0]})
     return log
 
 
