@@ -1,8 +1,8 @@
 """CPU oracle of the boundary network (test infrastructure only: used by tests to check the GPU
 kernels, never by the product path).
 
-Restates the network of the learned boundary -- 81 inputs, two hidden layers of 64 with exact
-GELU, one output -- and its mean-squared-error gradient, with the same roundings as the GPU
+Restates the network of the learned boundary -- 81 inputs, two hidden layers of 64 with the
+tanh-form GELU, one output -- and its mean-squared-error gradient, with the same roundings as the GPU
 kernels: inputs, W1, W2 and the first hidden activations rounded to BF16 (round to nearest
 even), everything else in float64 here (FP32 on the GPU).  The BF16 rounding is passed through
 as the identity in the backward pass, as the GPU does.  `fd_check` validates the backward
@@ -42,15 +42,18 @@ def bf16(a):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-_erf = np.vectorize(math.erf)
+_GC = math.sqrt(2.0 / math.pi)
+_GA = 0.044715
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    """GELU in the tanh form of Hendrycks & Gimpel (2016): z/2 (1 + tanh(sqrt(2/pi)(z + 0.044715 z^3)))."""
+    return 0.5 * z * (1.0 + np.tanh(_GC * (z + _GA * z ** 3)))
 
 
 def gelu_d(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(_GC * (z + _GA * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _GC * (1.0 + 3.0 * _GA * z * z)
 
 
 def forward(p, x, rounding=True):

@@ -40,11 +40,26 @@ __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi)
     return (uint32_t)f2bf(lo) | ((uint32_t)f2bf(hi) << 16);
 }
 
-// exact GELU and its derivative
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+// GELU in the tanh form of Hendrycks & Gimpel (2016), GELU(z) = z/2 (1 + tanh(u)),
+// u = sqrt(2/pi) (z + 0.044715 z^3), and its derivative; tanh from the hardware approximation
+// (tanh.approx.f32, relative error about 2^-11, below the BF16 rounding of the activations)
+__device__ __forceinline__ float tanh_hw(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float kGeluC = 0.7978845608028654f;  // sqrt(2/pi)
+constexpr float kGeluA = 0.044715f;
+__device__ __forceinline__ float gelu(float z)
+{
+    const float t = tanh_hw(kGeluC * fmaf(kGeluA * z, z * z, z));
+    return 0.5f * z * (1.f + t);
+}
 __device__ __forceinline__ float gelu_d(float z)
 {
-    return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+    const float t = tanh_hw(kGeluC * fmaf(kGeluA * z, z * z, z));
+    return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * kGeluC * fmaf(3.f * kGeluA, z * z, 1.f);
 }
 
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
@@ -418,7 +433,6 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
     uint16_t *xs = reinterpret_cast<uint16_t *>(smem + sizeof(NetSmem));
     uint16_t *h1 = xs + T * KP1;
     float *scale = reinterpret_cast<float *>(h1 + T * KP2);
-    float *xf = scale + T;  // [T][81] FP32 features before scaling
     load_net(s, net);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
     const int64_t plane = a.nxp * a.nz;
@@ -426,11 +440,13 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
         __syncthreads();
         // gather, one thread per node: feature (level l, neighbour (dz, dy, dx)) ->
         // l*27 + (dz+1)*9 + (dy+1)*3 + (dx+1); coordinates decoded once, the 27 loads of a level
-        // unrolled so that they are in flight together, sponge factors as 3+3+3 axis values
+        // unrolled so that they are in flight together, sponge factors as 3+3+3 axis values.
+        // Two passes over the same loads (the second from L1): the largest magnitude first,
+        // then the scaled BF16 features, so that no FP32 copy is staged in shared memory.
         {
             const int r = threadIdx.x;  // 128 threads, one row each
             const int64_t row = row0 + r;
-            float m = 0.f;
+            uint16_t *xr = xs + r * KP1;
             if (row < a.n) {
                 const int64_t q0 = a.nodes[row];
                 const int64_t iy = q0 / plane, rr = q0 - iy * plane, iz = rr / a.nxp, ix = rr - iz * a.nxp;
@@ -445,39 +461,40 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
                     fy[d] = (a.sx && oky[d]) ? __ldg(a.sy + iy + d - 1) : 1.f;
                     fz[d] = (a.sx && okz[d]) ? __ldg(a.sz + iz + d - 1) : 1.f;
                 }
+                // the 27 features of level l (level 1 carries its pending sponge factor)
+                auto level = [&](int l, float (&v)[27]) {
+                    const float *lv = l == 0 ? a.p_new : (l == 1 ? a.p_cur : a.hist);
+#pragma unroll
+                    for (int nb = 0; nb < 27; nb++) {
+                        const int dz = nb / 9, dy = (nb / 3) % 3, dx = nb % 3;
+                        const float x = (okx[dx] && oky[dy] && okz[dz])
+                                            ? lv[(ix + dx - 1) + (iz + dz - 1) * a.nxp + (iy + dy - 1) * plane]
+                                            : 0.f;
+                        v[nb] = l == 1 ? x * ((fx[dx] * fy[dy]) * fz[dz]) : x;
+                    }
+                };
+                float m = 0.f;
 #pragma unroll 1
                 for (int l = 0; l < 3; l++) {
-                    const float *lv = l == 0 ? a.p_new : (l == 1 ? a.p_cur : a.hist);
                     float v[27];
+                    level(l, v);
 #pragma unroll
-                    for (int nb = 0; nb < 27; nb++) {
-                        const int dz = nb / 9, dy = (nb / 3) % 3, dx = nb % 3;
-                        v[nb] = (okx[dx] && oky[dy] && okz[dz])
-                                    ? lv[(ix + dx - 1) + (iz + dz - 1) * a.nxp + (iy + dy - 1) * plane]
-                                    : 0.f;
-                    }
-#pragma unroll
-                    for (int nb = 0; nb < 27; nb++) {
-                        const int dz = nb / 9, dy = (nb / 3) % 3, dx = nb % 3;
-                        const float w = l == 1 ? v[nb] * ((fx[dx] * fy[dy]) * fz[dz]) : v[nb];
-                        xf[r * kMlpIn + l * 27 + nb] = w;
-                        m = fmaxf(m, fabsf(w));
-                    }
+                    for (int nb = 0; nb < 27; nb++) m = fmaxf(m, fabsf(v[nb]));
                 }
+                const float sc = m + 1e-30f;
+                scale[r] = sc;
+                const float inv = 1.f / sc;
+#pragma unroll 1
+                for (int l = 0; l < 3; l++) {
+                    float v[27];
+                    level(l, v);
+#pragma unroll
+                    for (int nb = 0; nb < 27; nb++) xr[l * 27 + nb] = f2bf(v[nb] * inv);
+                }
+                for (int k = kMlpIn; k < kMlpInPad; k++) xr[k] = 0;
             } else {
-                for (int f = 0; f < kMlpIn; f++) xf[r * kMlpIn + f] = 0.f;
-            }
-            scale[r] = m + 1e-30f;
-        }
-        __syncthreads();
-        {
-            const int r = threadIdx.x;
-            const float inv = 1.f / scale[r];
-#pragma unroll 8
-            for (int k = 0; k < kMlpInPad; k += 2) {
-                const float u0 = k < kMlpIn ? xf[r * kMlpIn + k] * inv : 0.f;
-                const float u1 = k + 1 < kMlpIn ? xf[r * kMlpIn + k + 1] * inv : 0.f;
-                *reinterpret_cast<uint32_t *>(xs + r * KP1 + k) = pack_bf2(u0, u1);
+                scale[r] = 1e-30f;
+                for (int k = 0; k < kMlpInPad; k++) xr[k] = 0;
             }
         }
         __syncthreads();
@@ -534,7 +551,7 @@ __global__ void k_gather_rows(const float *x, const float *t, const int64_t *idx
 size_t smem_forward() { return sizeof(NetSmem) + sizeof(uint16_t) * T * (KP1 + KP2); }
 size_t smem_train() { return smem_forward() + sizeof(TrainSmem); }
 size_t smem_w3() { return smem_forward() + sizeof(float) * (T * H + T + H); }
-size_t smem_abc() { return smem_forward() + sizeof(float) * (T + T * kMlpIn); }
+size_t smem_abc() { return smem_forward() + sizeof(float) * T; }
 
 int grid_for(int64_t n)
 {
@@ -602,9 +619,9 @@ cudaError_t abc_correction(const MlpDev &net, const AbcArgs &a, cudaStream_t s)
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    // persistent CTAs (two per SM fit the shared memory): the weights are staged once per CTA
+    // persistent CTAs (three per SM fit the shared memory): the weights are staged once per CTA
     const int64_t tiles = (a.n + T - 1) / T;
-    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 152 * 2), T, sm, s>>>(net, a);
+    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 152 * 3), T, sm, s>>>(net, a);
     return cudaGetLastError();
 }
 
