@@ -441,8 +441,8 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
         // gather, one thread per node: feature (level l, neighbour (dz, dy, dx)) ->
         // l*27 + (dz+1)*9 + (dy+1)*3 + (dx+1); coordinates decoded once, the 27 loads of a level
         // unrolled so that they are in flight together, sponge factors as 3+3+3 axis values.
-        // Two passes over the same loads (the second from L1): the largest magnitude first,
-        // then the scaled BF16 features, so that no FP32 copy is staged in shared memory.
+        // All 81 loads of a node are issued together and held in registers: the largest
+        // magnitude, then the scaled BF16 features (no FP32 copy in shared memory).
         {
             const int r = threadIdx.x;  // 128 threads, one row each
             const int64_t row = row0 + r;
@@ -473,24 +473,21 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
                         v[nb] = l == 1 ? x * ((fx[dx] * fy[dy]) * fz[dz]) : x;
                     }
                 };
-                float m = 0.f;
-#pragma unroll 1
-                for (int l = 0; l < 3; l++) {
-                    float v[27];
-                    level(l, v);
+                float v[3][27];
 #pragma unroll
-                    for (int nb = 0; nb < 27; nb++) m = fmaxf(m, fabsf(v[nb]));
-                }
+                for (int l = 0; l < 3; l++) level(l, v[l]);
+                float m = 0.f;
+#pragma unroll
+                for (int l = 0; l < 3; l++)
+#pragma unroll
+                    for (int nb = 0; nb < 27; nb++) m = fmaxf(m, fabsf(v[l][nb]));
                 const float sc = m + 1e-30f;
                 scale[r] = sc;
                 const float inv = 1.f / sc;
-#pragma unroll 1
-                for (int l = 0; l < 3; l++) {
-                    float v[27];
-                    level(l, v);
 #pragma unroll
-                    for (int nb = 0; nb < 27; nb++) xr[l * 27 + nb] = f2bf(v[nb] * inv);
-                }
+                for (int l = 0; l < 3; l++)
+#pragma unroll
+                    for (int nb = 0; nb < 27; nb++) xr[l * 27 + nb] = f2bf(v[l][nb] * inv);
                 for (int k = kMlpIn; k < kMlpInPad; k++) xr[k] = 0;
             } else {
                 scale[r] = 1e-30f;
