@@ -50,16 +50,20 @@ __device__ __forceinline__ float tanh_hw(float x)
     return y;
 }
 constexpr float kGeluC = 0.7978845608028654f;  // sqrt(2/pi)
-constexpr float kGeluA = 0.044715f;
+constexpr float kGeluCA = 0.7978845608028654f * 0.044715f;
+// u = z (c + c a z^2): two multiplies and one fma
+__device__ __forceinline__ float gelu_u(float z) { return z * fmaf(kGeluCA, z * z, kGeluC); }
 __device__ __forceinline__ float gelu(float z)
 {
-    const float t = tanh_hw(kGeluC * fmaf(kGeluA * z, z * z, z));
-    return 0.5f * z * (1.f + t);
+    const float t = tanh_hw(gelu_u(z));
+    const float h = 0.5f * z;
+    return fmaf(h, t, h);
 }
 __device__ __forceinline__ float gelu_d(float z)
 {
-    const float t = tanh_hw(kGeluC * fmaf(kGeluA * z, z * z, z));
-    return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * kGeluC * fmaf(3.f * kGeluA, z * z, 1.f);
+    // d/dz [z/2 (1 + tanh u)] = (1 + t)/2 + z/2 (1 - t^2) (c + 3 c a z^2)
+    const float t = tanh_hw(gelu_u(z));
+    return fmaf(0.5f, t, 0.5f) + (0.5f * z) * fmaf(-t, t, 1.f) * fmaf(3.f * kGeluCA, z * z, kGeluC);
 }
 
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
