@@ -109,20 +109,26 @@ def test_strip_correction_matches_oracle(semgb_lib, cuda_device):
 
 
 def test_trained_network_reduces_reflections(semgb_lib, cuda_device):
-    """Thin sponge (2 elements) with and without the trained network on the boundary nodes,
-    against a padded run: the network lowers the reflected energy in the interior."""
+    """Thin sponge (3 elements) with and without the trained network on the boundary nodes,
+    against a padded run: the network (best of its training rounds) lowers the reflected energy
+    in the interior, for the training source and for a source position not used in training.
+    Training is not bit-reproducible (gradients are summed with atomics); measured ratios are
+    0.3-0.45, the bound is 0.6."""
     semgb = semgb_lib
     from semgb import learned_boundary as LB
     from semgb import workloads as W
     c, h, o = 2000.0, 10.0, 4
     dt = W.cfl_dt(h, o, c)
-    s = LB.Setup(interior=6, sponge_t=2, order=o, h=h, c=c, pad=10, sponge_p=6, layer=0, f0=40.0, dt=dt,
-                 steps=260, src_frac=(0.25, 0.5, 0.5))
+    common = dict(interior=6, sponge_t=3, order=o, h=h, c=c, pad=12, sponge_p=6, layer=0, f0=40.0, dt=dt,
+                  steps=260)
+    s = LB.Setup(src_frac=(0.25, 0.5, 0.5), **common)
+    held = LB.Setup(src_frac=(0.6, 0.35, 0.55), **common)
     net = semgb.Mlp(3)
-    log = LB.train_network(s, net, rounds=2, epochs=10, per_step=3000, seed=0)
+    log = LB.train_network(s, net, rounds=3, epochs=10, per_step=3000, seed=0)
     print(log)
     assert log[0]["samples"] > 50000
-    e_plain, _ = LB.reflected_energy(s, None)
-    e_net, _ = LB.reflected_energy(s, net)
-    print(f"reflected energy: sponge only {e_plain:.3e}, sponge + network {e_net:.3e}")
-    assert e_net < 0.8 * e_plain
+    for setup in (s, held):
+        e_plain, _ = LB.reflected_energy(setup, None)
+        e_net, _ = LB.reflected_energy(setup, net)
+        print(f"reflected energy: sponge only {e_plain:.3e}, sponge + network {e_net:.3e}")
+        assert e_net < 0.6 * e_plain
