@@ -8,6 +8,8 @@
 //  k_mass     SEMsolver.cpp:33-36,74-80 assembled once: a_i = dt^2 / M_i
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace semgb {
@@ -98,9 +100,9 @@ __global__ void k_connectivity(int32_t *conn, int ex, int ez, int order, int64_t
 }
 
 // Elements adjacent to node index i along one axis with ne elements: [lo, hi].
-__device__ __forceinline__ void adj_range(int64_t i, int order, int ne, int64_t &lo, int64_t &hi)
+__device__ __forceinline__ void adj_range(int i, int order, int ne, int &lo, int &hi)
 {
-    const int64_t e = i / order;
+    const int e = i / order;
     if (i - e * order == 0) {
         lo = e > 0 ? e - 1 : 0;
         hi = e < ne ? e : ne - 1;
@@ -109,40 +111,52 @@ __device__ __forceinline__ void adj_range(int64_t i, int order, int ne, int64_t 
     }
 }
 
-__global__ void k_mass(float *a, const float *vel, const float *slow2, int ex, int ey, int ez,
-                       int order, int64_t nxp, const double *w, double detJ, double dt2)
+// 1 / c_e^2 per element, in double (the per-node sums below read it up to 8 times)
+__global__ void k_inv_c2(const float *vel, int64_t n, double *out)
 {
-    const int64_t nx = (int64_t)ex * order + 1, ny = (int64_t)ey * order + 1,
-                  nz = (int64_t)ez * order + 1, n = nxp * ny * nz;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t iy = q / (nxp * nz), r = q - iy * nxp * nz, iz = r / nxp, ix = r - iz * nxp;
-        if (ix >= nx) {
-            a[q] = 0.f;
-            continue;
-        }
-        // local weight of the node: w[i mod o] (element-boundary nodes have w_0 = w_o)
-        const double wq = w[ix % order] * w[iz % order] * w[iy % order];
-        int64_t x0, x1, z0, z1, y0, y1;
-        adj_range(ix, order, ex, x0, x1);
-        adj_range(iz, order, ez, z0, z1);
-        adj_range(iy, order, ey, y0, y1);
-        double m;
-        if (slow2) {
-            const double cnt = (double)((x1 - x0 + 1) * (z1 - z0 + 1) * (y1 - y0 + 1));
-            m = (double)slow2[q] * wq * detJ * cnt;
-        } else {
-            double sum = 0.0;
-            for (int64_t ey_ = y0; ey_ <= y1; ey_++)
-                for (int64_t ez_ = z0; ez_ <= z1; ez_++)
-                    for (int64_t ex_ = x0; ex_ <= x1; ex_++) {
-                        const double c = vel[ex_ + ez_ * ex + ey_ * (int64_t)ex * ez];
-                        sum += 1.0 / (c * c);
-                    }
-            m = wq * detJ * sum;
-        }
-        a[q] = (float)(dt2 / m);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double c = vel[i];
+        out[i] = 1.0 / (c * c);
     }
+}
+
+// a_i = dt^2 / M_i with M_i = w_i detJ sum over the adjacent elements of 1/c_e^2 (or, with a
+// node model, m_i w_i detJ times the number of adjacent elements), in double.  Grid: x-blocks of
+// a row by z by y (grid-stride over z and y), so node indices come without divisions.
+__global__ void k_mass(float *a, const double *inv_c2, const float *slow2, int ex, int ey, int ez, int order,
+                       int nxp, const double *w, double detJ, double dt2)
+{
+    const int nx = ex * order + 1, ny = ey * order + 1, nz = ez * order + 1;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ix >= nxp) return;
+    int x0 = 0, x1 = 0;
+    if (ix < nx) adj_range(ix, order, ex, x0, x1);
+    for (int iy = blockIdx.z; iy < ny; iy += gridDim.z)
+        for (int iz = blockIdx.y; iz < nz; iz += gridDim.y) {
+            const int64_t q = ix + (int64_t)nxp * (iz + (int64_t)nz * iy);
+            if (ix >= nx) {
+                a[q] = 0.f;
+                continue;
+            }
+            // local weight of the node: w[i mod o] (element-boundary nodes have w_0 = w_o)
+            const double wq = w[ix % order] * w[iz % order] * w[iy % order];
+            int z0, z1, y0, y1;
+            adj_range(iz, order, ez, z0, z1);
+            adj_range(iy, order, ey, y0, y1);
+            double m;
+            if (slow2) {
+                const double cnt = (double)((x1 - x0 + 1) * (z1 - z0 + 1) * (y1 - y0 + 1));
+                m = (double)slow2[q] * wq * detJ * cnt;
+            } else {
+                double sum = 0.0;
+                for (int ey_ = y0; ey_ <= y1; ey_++)
+                    for (int ez_ = z0; ez_ <= z1; ez_++)
+                        for (int ex_ = x0; ex_ <= x1; ex_++)
+                            sum += inv_c2[ex_ + (int64_t)ex * (ez_ + (int64_t)ez * ey_)];
+                m = wq * detJ * sum;
+            }
+            a[q] = (float)(dt2 / m);
+        }
 }
 
 // g_i <- g_i / m_i with m_i the node's squared slowness, recovered from the stored
@@ -161,10 +175,10 @@ __global__ void k_grad_scale(float *g, const float *a, int ex, int ey, int ez, i
             continue;
         }
         const double wq = w[ix % order] * w[iz % order] * w[iy % order];
-        int64_t x0, x1, z0, z1, y0, y1;
-        adj_range(ix, order, ex, x0, x1);
-        adj_range(iz, order, ez, z0, z1);
-        adj_range(iy, order, ey, y0, y1);
+        int x0, x1, z0, z1, y0, y1;
+        adj_range((int)ix, order, ex, x0, x1);
+        adj_range((int)iz, order, ez, z0, z1);
+        adj_range((int)iy, order, ey, y0, y1);
         const double W = wq * detJ * (double)((x1 - x0 + 1) * (z1 - z0 + 1) * (y1 - y0 + 1));
         g[q] = (float)((double)g[q] * (double)a[q] * W / dt2);
     }
@@ -208,8 +222,23 @@ cudaError_t launch_mass(float *a, const float *vel, const float *slow2, int ex, 
                         int order, int64_t nxp, const double *w_dev, double detJ, double dt2,
                         cudaStream_t s)
 {
-    k_mass<<<152 * 16, 256, 0, s>>>(a, vel, slow2, ex, ey, ez, order, nxp, w_dev, detJ, dt2);
-    return cudaGetLastError();
+    double *inv_c2 = nullptr;
+    if (!slow2) {
+        const int64_t ne = (int64_t)ex * ey * ez;
+        cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&inv_c2), ne * sizeof(double), s);
+        if (e != cudaSuccess) return e;
+        k_inv_c2<<<(unsigned)std::min<int64_t>((ne + 255) / 256, 152 * 16), 256, 0, s>>>(vel, ne, inv_c2);
+    }
+    const int64_t ny = (int64_t)ey * order + 1, nz = (int64_t)ez * order + 1;
+    const dim3 grid((unsigned)((nxp + 127) / 128), (unsigned)std::min<int64_t>(nz, 65535),
+                    (unsigned)std::min<int64_t>(ny, 65535));
+    k_mass<<<grid, 128, 0, s>>>(a, inv_c2, slow2, ex, ey, ez, order, (int)nxp, w_dev, detJ, dt2);
+    cudaError_t e = cudaGetLastError();
+    if (inv_c2) {
+        const cudaError_t f = cudaFreeAsync(inv_c2, s);
+        if (e == cudaSuccess) e = f;
+    }
+    return e;
 }
 
 }  // namespace semgb
