@@ -341,7 +341,8 @@ def run_ours(args):
             s.close()
             mesh.close()
             torch.cuda.synchronize()
-            line["rows"] = {"batched": measure_batched(), "uneven": measure_uneven(), "adjoint": measure_adjoint(),
+            line["rows"] = {"element_path": measure_element(args.elems, args.steps),
+                            "batched": measure_batched(), "uneven": measure_uneven(), "adjoint": measure_adjoint(),
                             "learned_boundary": measure_learned()}
         print(json.dumps(line), flush=True)
     s.close()
@@ -363,6 +364,35 @@ def _ev_time(stream, fn):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1)
+
+
+def measure_element(n: int = 200, steps: int = 20):
+    """The reference-shaped element path (SEM_KERNEL_ELEMENT: gather through the connectivity,
+    sum-factorised K_e.p, atomic scatter, then the update pass) on the headline workload:
+    node-steps/s and each kernel's fraction of the measured HBM bandwidth under its own byte
+    model (element pass: connectivity + gather + scatter read-modify-write; update: 24 B)."""
+    import torch
+    import semgb
+    wl = make_workload("c2", n)
+    mesh, s = semgb.solver_from_workload(wl, semgb.KERNEL_ELEMENT)
+    stream = torch.cuda.Stream()
+    s.set_stream(stream.cuda_stream)
+    N = mesh.n_nodes
+    steps = max(5, min(steps, 20))
+    s.step(3)
+    step_ms = _ev_time(stream, lambda: s.step(steps)) / steps
+    kms = [float(x) for x in s.time_kernels(steps)]
+    s.close()
+    mesh.close()
+    peak, peak_kind = hbm_peak()
+    eb = element_bytes_per_node(wl.order)
+    return {"workload": wl.name, "nodes": N, "steps": steps, "ms_per_step": step_ms,
+            "Gnode_steps_per_s": N / (step_ms / 1e3) / 1e9,
+            "element_kernel": {"ms": kms[1], "bytes_per_node": eb,
+                               "frac": eb * N / (kms[1] / 1e3) / 1e9 / peak},
+            "update_kernel": {"ms": kms[2], "bytes_per_node": 24.0,
+                              "frac": 24.0 * N / (kms[2] / 1e3) / 1e9 / peak},
+            "peak_kind": peak_kind}
 
 
 def measure_batched(steps: int = 40, n: int = 100, shots: int = 64):
@@ -607,7 +637,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=16, help="cpu_baseline steps")
     ap.add_argument("--ref-elems", type=int, default=32, help="--impl reference sub-box (elements per axis)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-rows", action="store_true", help="skip the batched / uneven / adjoint rows")
+    ap.add_argument("--no-rows", action="store_true", help="skip the element-path / batched / uneven / adjoint / learned-boundary rows")
     ap.add_argument("--case", choices=["batch40", "abc86"], default=None,
                     help="run a small fixed case for a kernel profile instead of the benchmark")
     args = ap.parse_args()
