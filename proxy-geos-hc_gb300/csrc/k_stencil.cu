@@ -42,7 +42,11 @@ namespace {
 #ifndef SEM_STENCIL_RW
 #define SEM_STENCIL_RW 2  // rows per warp instruction where the order allows it
 #endif
+#ifndef SEM_STENCIL_L2PF
+#define SEM_STENCIL_L2PF 2
+#endif
 constexpr int kLook = SEM_STENCIL_LOOKAHEAD;  // planes of lookahead
+constexpr int kL2Pf = SEM_STENCIL_L2PF;       // further planes prefetched into L2 (0: none)
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 constexpr int kTMax = kMaxOrder * (2 * kMaxOrder + 1);
 __constant__ float c_T[kMaxOrder][kTMax];  // [order-1][l * (2o+1) + d + o]
@@ -351,6 +355,16 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
         if (threadIdx.x == 0 && y + kLook <= ye - 1) {
             issue_ring(y + O + kLook);
             issue_aux(y + kLook);
+            if constexpr (kL2Pf > 0) {
+                // tiles kL2Pf planes beyond the shared-memory look-ahead, into L2; only boxes that
+                // lie inside the tensor (the window's halos are other CTAs' tiles)
+                const int pr = y + O + kLook + kL2Pf, pa = y + kLook + kL2Pf;
+                if (pr < ny) tma_prefetch_3d(rmap, x0, z0, ys + pr);
+                if (pa <= ye - 1) {
+                    tma_prefetch_3d(pmap, x0, z0, ys + pa);
+                    tma_prefetch_3d(amap, x0, z0, pa);
+                }
+            }
         }
         // gradient pass: the recorded K p' and the running gradient of the thread's nodes, loaded
         // before the waits so that their latency overlaps the plane's work
