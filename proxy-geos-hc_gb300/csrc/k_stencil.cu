@@ -33,8 +33,10 @@ namespace semgb {
 
 namespace {
 
+// Tiling knobs (compile-time; the defaults are the measured best on GB300, other values are
+// for sweeps: build.py -D NAME=value builds a separate library).
 #ifndef SEM_STENCIL_LOOKAHEAD
-#define SEM_STENCIL_LOOKAHEAD 1
+#define SEM_STENCIL_LOOKAHEAD 1  // planes loaded into shared memory ahead of the compute
 #endif
 #ifndef SEM_STENCIL_NG
 #define SEM_STENCIL_NG 2  // row groups per thread where the order allows it
@@ -43,7 +45,7 @@ namespace {
 #define SEM_STENCIL_RW 2  // rows per warp instruction where the order allows it
 #endif
 #ifndef SEM_STENCIL_L2PF
-#define SEM_STENCIL_L2PF 2
+#define SEM_STENCIL_L2PF 2  // planes beyond the look-ahead prefetched into L2
 #endif
 constexpr int kLook = SEM_STENCIL_LOOKAHEAD;  // planes of lookahead
 constexpr int kL2Pf = SEM_STENCIL_L2PF;       // further planes prefetched into L2 (0: none)
