@@ -91,7 +91,7 @@ def _loss(d, obs):
 
 
 def test_gradient_central_differences(semgb_lib, cuda_device):
-    """dL/dm along 4 seeded random directions against (L(m+eps dm) - L(m-eps dm)) / 2 eps,
+    """dL/dm along 8 seeded random directions against (L(m+eps dm) - L(m-eps dm)) / 2 eps,
     eps = 1e-3 relative."""
     semgb = semgb_lib
     n = 150
@@ -104,7 +104,7 @@ def test_gradient_central_differences(semgb_lib, cuda_device):
     assert loss > 0 and np.isfinite(g).all()
     rng = np.random.default_rng(11)
     eps = 1e-3
-    for k in range(4):
+    for k in range(8):
         dm = (m0 * rng.standard_normal(m0.shape)).astype(np.float64)
         lp = []
         for sgn in (1, -1):
