@@ -217,7 +217,8 @@ int sem_solver_time_kernels(sem_solver *s, int n_steps, float *ms);
  * the mesh, the velocity model, the sponge and the receiver set.  The shots' fields lie one
  * after another and one stencil pass steps them all, the CTAs of every shot of a tile running
  * together so that the mesh-side data (dt^2/M, sponge) is read from memory once per tile for
- * the batch.  Same conventions as sem_solver_*.
+ * the batch; each shot gets the same bits as a plain solver run of it in the default operator
+ * form (SEM_FORM_DIRECT, the only form of the batch).  Same conventions as sem_solver_*.
  * ------------------------------------------------------------------------------------------ */
 
 typedef struct sem_batch sem_batch;
