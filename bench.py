@@ -341,7 +341,7 @@ def run_ours(args):
             s.close()
             mesh.close()
             torch.cuda.synchronize()
-            line["rows"] = {"element_path": measure_element(args.elems, args.steps),
+            line["rows"] = {"orders": measure_orders(), "element_path": measure_element(args.elems, args.steps),
                             "batched": measure_batched(), "uneven": measure_uneven(), "adjoint": measure_adjoint(),
                             "learned_boundary": measure_learned()}
         print(json.dumps(line), flush=True)
@@ -364,6 +364,37 @@ def _ev_time(stream, fn):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1)
+
+
+def measure_orders(steps: int = 20, nodes_axis: int = 801):
+    """The stencil pass at every GLL order on boxes of about nodes_axis^3 nodes (constant 2000
+    m/s, 20-element sponge, one source): node-steps/s and the fraction of the measured HBM
+    bandwidth at 16 B per node (the headline recipe is order 4)."""
+    import torch
+    import semgb
+    from semgb import workloads as W
+    peak, _ = hbm_peak()
+    out = {}
+    for o in (1, 2, 3, 4, 5):
+        e = (nodes_axis - 1) // o
+        h = 10.0
+        mesh = semgb.Mesh(e, e, e, e * h, e * h, e * h, o)
+        mesh.set_velocity(np.full(e ** 3, 2000.0, np.float32))
+        dt = W.cfl_dt(h, o, 2000.0)
+        s = semgb.Solver(mesh, dt)
+        s.set_kernel(semgb.KERNEL_STENCIL)
+        stream = torch.cuda.Stream()
+        s.set_stream(stream.cuda_stream)
+        s.set_sponge(min(20, e // 4), 0.06)
+        s.set_source_points(np.array([[e * h / 2] * 3], np.float32), semgb.ricker(steps + 8, dt, 10.0, 1)[None])
+        s.step(4)
+        ms = _ev_time(stream, lambda: s.step(steps)) / steps
+        N = mesh.n_nodes
+        out[f"q{o}"] = {"elements": e, "nodes": N, "ms_per_step": ms, "Gnode_steps_per_s": N / (ms / 1e3) / 1e9,
+                        "frac": 16.0 * N / (ms / 1e3) / 1e9 / peak}
+        s.close()
+        mesh.close()
+    return out
 
 
 def measure_element(n: int = 200, steps: int = 20):

@@ -61,7 +61,9 @@ struct Cfg {
     // with the same z-local index (warp-uniform coefficients).  Narrow tiles waste fewer lanes
     // on the last x-tile of a row (801 nodes: 13 tiles of 64 against 7 of 128; 289 nodes at
     // o = 3: 7 of 48 against 4 of 96); the groups share one thread's per-plane bookkeeping
-    // (waits, slot selection, coefficient dispatch, sponge).  Order 5: one row per warp, 8 warps.
+    // (waits, slot selection, coefficient dispatch, sponge).  Order 5: one row per warp, 8
+    // warps (5 warps on row pairs, 80 x 10 tiles, measured slower: 219.7 against 234.5
+    // Gnode-steps/s at 801^3 nodes).
     static constexpr bool SPLIT = O <= 4;
     static constexpr int NG = SPLIT ? SEM_STENCIL_NG : 1;  // row groups per thread
     static constexpr int WARPS = !SPLIT ? 8 : (O == 3 ? 3 : 8 / NG);
