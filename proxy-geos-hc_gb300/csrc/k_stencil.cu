@@ -61,13 +61,14 @@ struct Cfg {
     // with the same z-local index (warp-uniform coefficients).  Narrow tiles waste fewer lanes
     // on the last x-tile of a row (801 nodes: 13 tiles of 64 against 7 of 128; 289 nodes at
     // o = 3: 7 of 48 against 4 of 96); the groups share one thread's per-plane bookkeeping
-    // (waits, slot selection, coefficient dispatch, sponge).  Order 5: one row per warp, 8
-    // warps (5 warps on row pairs, 80 x 10 tiles, measured slower: 219.7 against 234.5
-    // Gnode-steps/s at 801^3 nodes).
+    // (waits, slot selection, coefficient dispatch, sponge).  Order 5: 5 warps, four rows per
+    // warp instruction (8 lanes each), one group, tiles of 40 x 20 (801^3 nodes: 242.8
+    // Gnode-steps/s, against 234.5 with one row per warp and 8 warps on 160 x 8 tiles and 219.7
+    // with row pairs on 80 x 10 tiles).
     static constexpr bool SPLIT = O <= 4;
     static constexpr int NG = SPLIT ? SEM_STENCIL_NG : 1;  // row groups per thread
-    static constexpr int WARPS = !SPLIT ? 8 : (O == 3 ? 3 : 8 / NG);
-    static constexpr int RW = SPLIT ? SEM_STENCIL_RW : 1;
+    static constexpr int WARPS = !SPLIT ? 5 : (O == 3 ? 3 : 8 / NG);
+    static constexpr int RW = SPLIT ? SEM_STENCIL_RW : 4;
     static constexpr int LANES = 32 / RW;               // lanes per row
     static constexpr int GR = O * RW;                   // rows between a thread's groups
     static constexpr int TZ = WARPS * RW * NG;          // rows per CTA
