@@ -342,7 +342,8 @@ def run_ours(args):
             mesh.close()
             torch.cuda.synchronize()
             line["rows"] = {"orders": measure_orders(), "element_path": measure_element(args.elems, args.steps),
-                            "batched": measure_batched(), "uneven": measure_uneven(), "adjoint": measure_adjoint(),
+                            "batched": measure_batched(), "uneven": measure_uneven(),
+                            "uneven_small": measure_uneven(200, 8, 24, "c3_uneven_32_small"), "adjoint": measure_adjoint(),
                             "learned_boundary": measure_learned()}
         print(json.dumps(line), flush=True)
     s.close()
@@ -469,14 +470,14 @@ def measure_batched(steps: int = 40, n: int = 100, shots: int = 64):
             "batched_GBps": batch * (12.0 + 4.0 / shots)}
 
 
-def measure_uneven(steps: int = 20):
-    """32 independent problems (per-axis elements in [40, 120], orders {2, 3, 4}) advanced as one
+def measure_uneven(steps: int = 20, lo: int = 40, hi: int = 120, name: str = "c3_uneven_32"):
+    """32 independent problems (per-axis elements in [lo, hi], orders {2, 3, 4}) advanced as one
     group (one multi-branch CUDA graph per two steps) against the same solvers stepped one after
     another: node-steps/s over the whole batch."""
     import torch
     import semgb
     from semgb import workloads as W
-    wls = W.c3_uneven_batch(32, 800)
+    wls = W.c3_uneven_batch(32, 800, lo=lo, hi=hi)
     stream = torch.cuda.Stream()
     members = [semgb.solver_from_workload(w, semgb.KERNEL_STENCIL) for w in wls]
     nodes = sum(m.n_nodes for m, _ in members)
@@ -493,7 +494,7 @@ def measure_uneven(steps: int = 20):
     for m, s in members:
         s.close()
         m.close()
-    return {"workload": "c3_uneven_32", "problems": len(wls), "nodes": nodes, "steps": steps,
+    return {"workload": name, "problems": len(wls), "elements_per_axis": [lo, hi], "nodes": nodes, "steps": steps,
             "orders": sorted({w.order for w in wls}),
             "group_Gnode_steps_per_s": nodes * steps / (grp_ms / 1e3) / 1e9,
             "sequential_Gnode_steps_per_s": nodes * steps / (seq_ms / 1e3) / 1e9,
