@@ -22,6 +22,8 @@
 //   F  y = yx + yz + yy scattered with red.global.add.f32 through the connectivity
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace semgb {
@@ -37,7 +39,7 @@ struct ElemCfg {
     static constexpr int CS = NPE | 1;  // odd row stride: lanes hit distinct banks
     static constexpr int THREADS = TE * NP;
     static constexpr int MINB = O == 1 ? 8 : O == 2 ? 5 : O == 3 ? 3 : O == 4 ? 2 : 2;
-    static constexpr size_t SMEM = sizeof(int) * TE * CS + sizeof(float) * NPE * TE * 2 +
+    static constexpr size_t SMEM = sizeof(int) * 2 * TE * CS + sizeof(float) * NPE * TE * 2 +
                                    sizeof(float) * 3 * NP;
 };
 
@@ -72,80 +74,112 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     using C = ElemCfg<O>;
     constexpr int O1 = C::O1, NP = C::NP, NPE = C::NPE, CS = C::CS, TE = C::TE;
     extern __shared__ __align__(16) unsigned char smem[];
-    int *s_conn = reinterpret_cast<int *>(smem);
-    float *s_p = reinterpret_cast<float *>(s_conn + TE * CS);
+    int *s_conn = reinterpret_cast<int *>(smem);  // [2][TE * CS]: this tile's rows and the next tile's
+    float *s_p = reinterpret_cast<float *>(s_conn + 2 * TE * CS);
     float *s_y = s_p + NPE * TE;
     float *s_tab = s_y + NPE * TE;
 
     // "lane" = element of the tile, "warp" = pencil (a hardware warp when TE == 32)
     const int tid = threadIdx.x, lane = tid % TE, warp = tid / TE;
-    const int64_t e0 = (int64_t)blockIdx.x * TE;
-    const int ne = (int)min((int64_t)TE, a.n_elem - e0);
+    const int64_t ntiles = (a.n_elem + TE - 1) / TE;
+    int64_t t = blockIdx.x;
+    if (t >= ntiles) return;
 
-    // A: coefficient table and connectivity rows
-    for (int q = tid; q < 3 * NP; q += C::THREADS) s_tab[q] = __ldg(a.tab + q);
-    {
+    // connectivity rows of tile u (contiguous in HBM) into buffer b, coalesced
+    auto load_conn = [&](int64_t u, int b) {
+        const int64_t e0 = u * TE;
+        const int ne = (int)min((int64_t)TE, a.n_elem - e0);
         const int32_t *cg = a.conn + e0 * NPE;
-        const int total = ne * NPE;
-        for (int q = tid; q < total; q += C::THREADS) {
+        int *dst = s_conn + b * TE * CS;
+        for (int q = tid; q < ne * NPE; q += C::THREADS) {
             const int e = q / NPE;
-            s_conn[e * CS + (q - e * NPE)] = __ldg(cg + q);
+            dst[e * CS + (q - e * NPE)] = __ldg(cg + q);
         }
-    }
-    __syncthreads();
+    };
+    // the thread's x-pencil (local j, k fixed) of tile u through buffer b
+    const int jx = warp % O1, kx = warp / O1;
+    auto gather = [&](int64_t u, int b, float (&v)[O1]) {
+        const bool act = lane < (int)min((int64_t)TE, a.n_elem - u * TE);
+        const int *cr = s_conn + b * TE * CS + lane * CS;
+#pragma unroll
+        for (int i = 0; i < O1; i++) v[i] = act ? __ldg(a.p + cr[i + O1 * jx + NP * kx]) : 0.f;
+    };
 
-    const bool act = lane < ne;
-    // B: gather the thread's x-pencil (local j, k fixed)
-    float px[O1];
-    {
-        const int j = warp % O1, k = warp / O1;
+    // A: coefficient table, the first tile's rows, and its pencil values
+    for (int q = tid; q < 3 * NP; q += C::THREADS) s_tab[q] = __ldg(a.tab + q);
+    load_conn(t, 0);
+    __syncthreads();
+    float pn[O1];
+    gather(t, 0, pn);
+
+    // Persistent loop: while a tile runs its z- and y-directions and its scatter, the next
+    // tile's connectivity rows are in shared memory and its pencil values are in flight.
+    for (int b = 0; t < ntiles; t += gridDim.x, b ^= 1) {
+        const int64_t tn = t + gridDim.x;
+        const bool act = lane < (int)min((int64_t)TE, a.n_elem - t * TE);
+        // B: this tile's pencil values into shared memory; the next tile's rows into the other buffer
+        float px[O1];
 #pragma unroll
         for (int i = 0; i < O1; i++) {
-            const int node = i + O1 * j + NP * k;
-            float v = 0.f;
-            if (act) v = __ldg(a.p + s_conn[lane * CS + node]);
-            px[i] = v;
-            s_p[node * TE + lane] = v;
+            px[i] = pn[i];
+            s_p[(i + O1 * jx + NP * kx) * TE + lane] = px[i];
         }
-    }
-    // C: x-direction in registers
-    float yx[O1];
-    {
-        const int j = warp % O1, k = warp / O1;
-        pencil_apply<O>(a, px, s_tab[0 * NP + j + O1 * k], yx);
-    }
-    __syncthreads();
-    // D: z-direction (local index j varies)
-    {
-        const int i = warp % O1, k = warp / O1;
-        float pz[O1], yz[O1];
+        if (tn < ntiles) load_conn(tn, b ^ 1);
+        // C: x-direction in registers
+        float yx[O1];
+        pencil_apply<O>(a, px, s_tab[0 * NP + jx + O1 * kx], yx);
+        __syncthreads();
+        if (tn < ntiles) gather(tn, b ^ 1, pn);
+        // D: z-direction (local index j varies)
+        {
+            const int i = warp % O1, k = warp / O1;
+            float pz[O1], yz[O1];
 #pragma unroll
-        for (int m = 0; m < O1; m++) pz[m] = s_p[(i + O1 * m + NP * k) * TE + lane];
-        pencil_apply<O>(a, pz, s_tab[1 * NP + i + O1 * k], yz);
+            for (int m = 0; m < O1; m++) pz[m] = s_p[(i + O1 * m + NP * k) * TE + lane];
+            pencil_apply<O>(a, pz, s_tab[1 * NP + i + O1 * k], yz);
 #pragma unroll
-        for (int m = 0; m < O1; m++) s_y[(i + O1 * m + NP * k) * TE + lane] = yz[m];
-    }
-    __syncthreads();
-    // E: y-direction (local index k varies); each thread overwrites only its own pencil of s_p
-    {
-        const int i = warp % O1, j = warp / O1;
-        float py[O1], yy[O1];
-#pragma unroll
-        for (int n = 0; n < O1; n++) py[n] = s_p[(i + O1 * j + NP * n) * TE + lane];
-        pencil_apply<O>(a, py, s_tab[2 * NP + i + O1 * j], yy);
-#pragma unroll
-        for (int n = 0; n < O1; n++) s_p[(i + O1 * j + NP * n) * TE + lane] = yy[n];
-    }
-    __syncthreads();
-    // F: scatter through the connectivity
-    if (act) {
-        const int j = warp % O1, k = warp / O1;
-#pragma unroll
-        for (int i = 0; i < O1; i++) {
-            const int node = i + O1 * j + NP * k;
-            const float v = yx[i] + s_y[node * TE + lane] + s_p[node * TE + lane];
-            atomicAdd(a.y + s_conn[lane * CS + node], v);  // result unused: compiles to RED
+            for (int m = 0; m < O1; m++) s_y[(i + O1 * m + NP * k) * TE + lane] = yz[m];
         }
+        __syncthreads();
+        // E: y-direction (local index k varies); each thread overwrites only its own pencil of s_p
+        {
+            const int i = warp % O1, j = warp / O1;
+            float py[O1], yy[O1];
+#pragma unroll
+            for (int n = 0; n < O1; n++) py[n] = s_p[(i + O1 * j + NP * n) * TE + lane];
+            pencil_apply<O>(a, py, s_tab[2 * NP + i + O1 * j], yy);
+#pragma unroll
+            for (int n = 0; n < O1; n++) s_p[(i + O1 * j + NP * n) * TE + lane] = yy[n];
+        }
+        __syncthreads();
+        // F: scatter through the connectivity.  The tile's elements are consecutive (one per
+        // lane); where the next lane's element shares this element's right x-face (same global
+        // nodes), its left-face value is added here with a shuffle and it skips that atomic.
+        {
+            const int *cr = s_conn + b * TE * CS + lane * CS;
+            float v[O1];
+#pragma unroll
+            for (int i = 0; i < O1; i++) {
+                const int node = i + O1 * jx + NP * kx;
+                v[i] = act ? yx[i] + s_y[node * TE + lane] + s_p[node * TE + lane] : 0.f;
+            }
+            const int g_left = act ? cr[0 + O1 * jx + NP * kx] : -1;
+            const int g_right = act ? cr[O + O1 * jx + NP * kx] : -2;
+            const float v_next = __shfl_down_sync(0xffffffffu, v[0], 1, TE);
+            const int g_next = __shfl_down_sync(0xffffffffu, g_left, 1, TE);
+            const int g_prev = __shfl_up_sync(0xffffffffu, g_right, 1, TE);
+            const bool merge_next = lane + 1 < TE && g_next == g_right;
+            const bool merged_into_prev = lane > 0 && g_prev == g_left;
+            if (merge_next) v[O] += v_next;
+            if (act) {
+#pragma unroll
+                for (int i = 0; i < O1; i++) {
+                    if (i == 0 && merged_into_prev) continue;
+                    atomicAdd(a.y + cr[i + O1 * jx + NP * kx], v[i]);  // result unused: compiles to RED
+                }
+            }
+        }
+        __syncthreads();  // s_p, s_y and this tile's rows are reused by the next iteration
     }
 }
 
@@ -154,8 +188,17 @@ cudaError_t launch_element_t(const ElementArgs &a, cudaStream_t s)
 {
     using C = ElemCfg<O>;
     if (a.n_elem <= 0) return cudaSuccess;
-    const int64_t grid = (a.n_elem + C::TE - 1) / C::TE;
-    if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const int64_t tiles = (a.n_elem + C::TE - 1) / C::TE;
+    // persistent CTAs: as many as are resident at once
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_element<O>, C::THREADS, C::SMEM) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    const int64_t grid = std::min<int64_t>(tiles, (int64_t)sms * per_sm);
     k_element<O><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(a);
     return cudaGetLastError();
 }
