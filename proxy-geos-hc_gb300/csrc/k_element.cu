@@ -18,7 +18,7 @@
 //   B  gather p through the rows: each thread loads its x-pencil (registers + shared copy)
 //   C  x-direction contraction in registers
 //   D  z-direction (xi2) pencils from shared, result -> s_y
-//   E  y-direction (xi3) pencils from shared, result overwrites the thread's own pencil in s_p
+//   E  y-direction (xi3) pencils from shared, result -> s_w (no barrier after D: both only read s_p)
 //   F  y = yx + yz + yy scattered with red.global.add.f32 through the connectivity
 #include <cuda_runtime.h>
 
@@ -39,7 +39,7 @@ struct ElemCfg {
     static constexpr int CS = NPE | 1;  // odd row stride: lanes hit distinct banks
     static constexpr int THREADS = TE * NP;
     static constexpr int MINB = O == 1 ? 8 : O == 2 ? 5 : O == 3 ? 3 : O == 4 ? 2 : 2;
-    static constexpr size_t SMEM = sizeof(int) * 2 * TE * CS + sizeof(float) * NPE * TE * 2 +
+    static constexpr size_t SMEM = sizeof(int) * 2 * TE * CS + sizeof(float) * NPE * TE * 3 +
                                    sizeof(float) * 3 * NP;
 };
 
@@ -76,8 +76,9 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     extern __shared__ __align__(16) unsigned char smem[];
     int *s_conn = reinterpret_cast<int *>(smem);  // [2][TE * CS]: this tile's rows and the next tile's
     float *s_p = reinterpret_cast<float *>(s_conn + 2 * TE * CS);
-    float *s_y = s_p + NPE * TE;
-    float *s_tab = s_y + NPE * TE;
+    float *s_y = s_p + NPE * TE;  // z-direction results
+    float *s_w = s_y + NPE * TE;  // y-direction results
+    float *s_tab = s_w + NPE * TE;
 
     // "lane" = element of the tile, "warp" = pencil (a hardware warp when TE == 32)
     const int tid = threadIdx.x, lane = tid % TE, warp = tid / TE;
@@ -130,7 +131,8 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
         pencil_apply<O>(a, px, s_tab[0 * NP + jx + O1 * kx], yx);
         __syncthreads();
         if (tn < ntiles) gather(tn, b ^ 1, pn);
-        // D: z-direction (local index j varies)
+        // D: z-direction (local index j varies) into s_y, and E: y-direction (local index k
+        // varies) into s_w; both only read s_p, so no barrier between them
         {
             const int i = warp % O1, k = warp / O1;
             float pz[O1], yz[O1];
@@ -140,8 +142,6 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
 #pragma unroll
             for (int m = 0; m < O1; m++) s_y[(i + O1 * m + NP * k) * TE + lane] = yz[m];
         }
-        __syncthreads();
-        // E: y-direction (local index k varies); each thread overwrites only its own pencil of s_p
         {
             const int i = warp % O1, j = warp / O1;
             float py[O1], yy[O1];
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
             for (int n = 0; n < O1; n++) py[n] = s_p[(i + O1 * j + NP * n) * TE + lane];
             pencil_apply<O>(a, py, s_tab[2 * NP + i + O1 * j], yy);
 #pragma unroll
-            for (int n = 0; n < O1; n++) s_p[(i + O1 * j + NP * n) * TE + lane] = yy[n];
+            for (int n = 0; n < O1; n++) s_w[(i + O1 * j + NP * n) * TE + lane] = yy[n];
         }
         __syncthreads();
         // F: scatter through the connectivity.  The tile's elements are consecutive (one per
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
 #pragma unroll
             for (int i = 0; i < O1; i++) {
                 const int node = i + O1 * jx + NP * kx;
-                v[i] = act ? yx[i] + s_y[node * TE + lane] + s_p[node * TE + lane] : 0.f;
+                v[i] = act ? yx[i] + s_y[node * TE + lane] + s_w[node * TE + lane] : 0.f;
             }
             const int g_left = act ? cr[0 + O1 * jx + NP * kx] : -1;
             const int g_right = act ? cr[O + O1 * jx + NP * kx] : -2;
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
                 }
             }
         }
-        __syncthreads();  // s_p, s_y and this tile's rows are reused by the next iteration
+        __syncthreads();  // s_p, s_y, s_w and this tile's rows are reused by the next iteration
     }
 }
 
