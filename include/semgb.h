@@ -62,6 +62,12 @@ typedef struct sem_solver sem_solver;
 const char *sem_last_error_string(void);
 int sem_version(void); /* major*10000 + minor*100 + patch */
 
+/* Self-test of the bounded device waits the kernels use: one CTA waits on an mbarrier phase that
+ * nothing completes (no arrival, no copy in flight), so the wait ends at its limit
+ * (limit_seconds in (0, 2]); returns SEM_ERR_TIMEOUT with the time waited, and the context stays
+ * usable.  Returns SEM_OK only if the wait completed, which would be a defect. */
+int sem_selftest_bounded_wait(double limit_seconds, double *waited_seconds);
+
 /* ------------------------------------------------------------------------------------------
  * Host-only utilities (no GPU needed).
  * ------------------------------------------------------------------------------------------ */

@@ -14,6 +14,7 @@
 #include "abi.h"
 #include "solver.h"
 #include "stencil.h"
+#include "tma.cuh"
 
 using namespace semgb;
 
@@ -66,11 +67,57 @@ int solver_set_raw_sources(sem_solver *s, int n_src, const int64_t *nodes, const
     return SEM_OK;
 }
 
+namespace {
+
+// One CTA waits on an mbarrier phase that nothing completes (no arrival, no copy), so the
+// bounded wait can only end at its limit; thread 0 reports the outcome and the time waited.
+__global__ void k_wait_selftest(uint64_t limit_ns, int *status, unsigned long long *waited_ns)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        semgb::bar_init(&bar, 1);
+        semgb::fence_barrier_init();
+    }
+    __syncthreads();
+    const uint64_t t0 = semgb::global_ns();
+    const bool done = semgb::bar_wait(&bar, 0, limit_ns);
+    if (threadIdx.x == 0) {
+        *status = done ? 0 : 1;
+        *waited_ns = (unsigned long long)(semgb::global_ns() - t0);
+    }
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *sem_last_error_string(void) { return g_err.c_str(); }
 
 int sem_version(void) { return 100; }
+
+int sem_selftest_bounded_wait(double limit_seconds, double *waited_seconds)
+{
+    if (!(limit_seconds > 0) || limit_seconds > 2.0) return fail(SEM_ERR_ARG, "limit_seconds must be in (0, 2]");
+    int *d_status = nullptr;
+    unsigned long long *d_ns = nullptr;
+    CUDA_TRY(dalloc(&d_status, 1));
+    cudaError_t e = dalloc(&d_ns, 1);
+    if (e == cudaSuccess) {
+        k_wait_selftest<<<1, 32>>>((uint64_t)(limit_seconds * 1e9), d_status, d_ns);
+        e = cudaGetLastError();
+    }
+    int status = 0;
+    unsigned long long ns = 0;
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&ns, d_ns, sizeof(ns), cudaMemcpyDeviceToHost);
+    dfree(d_status);
+    dfree(d_ns);
+    if (e != cudaSuccess) return fail(SEM_ERR_CUDA, cudaGetErrorString(e));
+    if (waited_seconds) *waited_seconds = ns * 1e-9;
+    if (status != 0) return fail(SEM_ERR_TIMEOUT, "bounded wait gave up at its limit (self-test)");
+    return SEM_OK;
+}
 
 // ----------------------------------------------------------------------------------------------
 // host-only utilities

@@ -40,6 +40,7 @@ class SemError(RuntimeError):
 _SIGS = {
     "sem_last_error_string": [],
     "sem_version": [],
+    "sem_selftest_bounded_wait": [C.c_double, C.POINTER(C.c_double)],
     "sem_gll_tables": [C.c_int, _F64P, _F64P, _F64P],
     "sem_ricker": [C.c_int, C.c_float, C.c_float, C.c_int, _F32P],
     "sem_box_counts": [C.c_int, C.c_int, C.c_int, C.c_int, _I64P, _I64P, _I64P],
@@ -718,3 +719,12 @@ class Adjoint:
         out = np.zeros((self.n_steps, self.n_adj_rec), np.float32)
         _check(lib().sem_adjoint_get_adjoint_traces(self._h, _p(out, _F32P)))
         return out
+
+
+def selftest_bounded_wait(limit_seconds: float = 0.05):
+    """Run the bounded-wait self-test (sem_selftest_bounded_wait): a device wait on an mbarrier
+    phase that nothing completes.  Returns (status code, seconds waited); the expected code is
+    SEM_ERR_TIMEOUT."""
+    waited = C.c_double(0.0)
+    rc = lib().sem_selftest_bounded_wait(float(limit_seconds), C.byref(waited))
+    return int(rc), float(waited.value)

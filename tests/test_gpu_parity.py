@@ -271,3 +271,21 @@ def test_many_sources_vs_oracle(semgb_lib, cuda_device, repeat):
     s.step(30)
     assert rel_l2(s.pressure(), r32[0]) < 1e-5
     assert rel_l2(s.traces(), r32[2]) < 1e-5
+
+
+def test_bounded_wait_gives_up_and_reports(semgb_lib, cuda_device):
+    """Failure detection on the device: a wait on an mbarrier phase that nothing completes (the
+    same bounded wait the stencil pass uses on its TMA tiles) ends at its limit, the host gets
+    SEM_ERR_TIMEOUT, and the context stays usable (a solver run afterwards matches one before)."""
+    from semgb import workloads as W
+    semgb = semgb_lib
+    wl = W.small_random(6, 5, 4, 4, 20, seed=12, nsrc=1, nrec=5)
+    mesh, s = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
+    s.step(20)
+    before = s.traces()
+    rc, waited = semgb.selftest_bounded_wait(0.05)
+    assert rc == semgb.SEM_ERR_TIMEOUT
+    assert 0.05 <= waited < 1.0
+    mesh2, s2 = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
+    s2.step(20)
+    assert np.array_equal(s2.traces(), before)
