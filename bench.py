@@ -341,7 +341,7 @@ def run_ours(args):
             s.close()
             mesh.close()
             torch.cuda.synchronize()
-            line["rows"] = {"orders": measure_orders(), "element_path": measure_element(args.elems, args.steps),
+            line["rows"] = {"operator_forms": measure_forms(args.elems), "orders": measure_orders(), "element_path": measure_element(args.elems, args.steps),
                             "batched": measure_batched(), "uneven": measure_uneven(),
                             "uneven_small": measure_uneven(200, 8, 24, "c3_uneven_32_small"), "adjoint": measure_adjoint(),
                             "learned_boundary": measure_learned()}
@@ -365,6 +365,26 @@ def _ev_time(stream, fn):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1)
+
+
+def measure_forms(n: int = 200, steps: int = 20):
+    """Both operator forms of the stencil pass on the headline workload: node-steps/s of the
+    direct form (default) and of the difference form (sem_solver_set_operator_form)."""
+    import torch
+    import semgb
+    wl = make_workload("c2", n)
+    out = {}
+    for name, form in (("direct", semgb.FORM_DIRECT), ("difference", semgb.FORM_DIFFERENCE)):
+        mesh, s = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
+        s.set_operator_form(form)
+        stream = torch.cuda.Stream()
+        s.set_stream(stream.cuda_stream)
+        s.step(4)
+        ms = _ev_time(stream, lambda: s.step(steps)) / steps
+        out[name] = {"ms_per_step": ms, "Gnode_steps_per_s": mesh.n_nodes / (ms / 1e3) / 1e9}
+        s.close()
+        mesh.close()
+    return out
 
 
 def measure_orders(steps: int = 20, nodes_axis: int = 801):
