@@ -643,7 +643,9 @@ def measure_learned(steps_time: int = 40):
 
 def run_case(name: str):
     """Small fixed cases for kernel profiles (no JSON line): `batch40` steps a 64-shot batch on a
-    40^3 Q4 mesh 6 times; `abc86` runs 6 steps of an 86^3 Q4 mesh with the boundary network."""
+    40^3 Q4 mesh 6 times; `abc86` runs 6 steps of an 86^3 Q4 mesh with the boundary network;
+    `q5_80` runs 6 stencil steps of an 80^3 order-5 box (401^3 nodes, constant 2000 m/s,
+    20-element sponge, one source)."""
     import semgb
     from semgb import workloads as W
     if name == "batch40":
@@ -672,6 +674,18 @@ def run_case(name: str):
         abc.step(6)
         sol.synchronize()
         print("abc86 ok", abc.n_nodes)
+    elif name == "q5_80":
+        ne, o, h, c = 80, 5, 10.0, 2000.0
+        dt = W.cfl_dt(h, o, c)
+        mesh = semgb.Mesh(ne, ne, ne, ne * h, ne * h, ne * h, o)
+        mesh.set_velocity(np.full(ne ** 3, c, np.float32))
+        sol = semgb.Solver(mesh, dt)
+        sol.set_kernel(semgb.KERNEL_STENCIL)
+        sol.set_sponge(20, 0.06)
+        sol.set_source_points(np.array([[ne * h / 2] * 3], np.float32), semgb.ricker(200, dt, 10.0, 1)[None])
+        sol.step(6)
+        sol.synchronize()
+        print("q5_80 ok", mesh.n_nodes)
     else:
         raise SystemExit(f"unknown case {name}")
 
@@ -690,7 +704,7 @@ def main():
     ap.add_argument("--ref-elems", type=int, default=32, help="--impl reference sub-box (elements per axis)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-rows", action="store_true", help="skip the element-path / batched / uneven / adjoint / learned-boundary rows")
-    ap.add_argument("--case", choices=["batch40", "abc86"], default=None,
+    ap.add_argument("--case", choices=["batch40", "abc86", "q5_80"], default=None,
                     help="run a small fixed case for a kernel profile instead of the benchmark")
     args = ap.parse_args()
     if args.case:

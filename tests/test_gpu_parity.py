@@ -289,3 +289,60 @@ def test_bounded_wait_gives_up_and_reports(semgb_lib, cuda_device):
     mesh2, s2 = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
     s2.step(20)
     assert np.array_equal(s2.traces(), before)
+
+
+# Boxes spanning several CTA tiles along x and z with a ragged last tile (x by z tiles of the
+# stencil pass: 16 x 16, 32 x 16, 48 x 12, 64 x 16, 40 x 20 nodes for orders 1-5) and cut into
+# several y-chunks, the last one shorter.
+MULTI_TILE = {1: (150, 33, 100), 2: (75, 15, 40), 3: (50, 10, 25), 4: (38, 8, 20), 5: (30, 6, 16)}
+_multi_tile_oracle = {}
+
+
+def _multi_tile_case(order):
+    """Workload, seeded smooth initial levels and the oracle's FP32 and FP64 results after 10
+    steps (computed once per order)."""
+    from oracle import oracle as O
+    from semgb import workloads as W
+    if order not in _multi_tile_oracle:
+        ex, ey, ez = MULTI_TILE[order]
+        wl = W.small_random(ex, ey, ez, order, 10, seed=300 + order, nsrc=3, nrec=24)
+        P = O.problem_from_workload(wl, 10)
+        N = P.n_nodes
+        nx, ny, nz = ex * order + 1, ey * order + 1, ez * order + 1
+        iy, iz, ix = np.unravel_index(np.arange(N), (ny, nz, nx))
+        base = np.sin(0.3 * ix + 0.2) * np.cos(0.25 * iz) * np.sin(0.2 * iy + 0.5)
+        rng = np.random.default_rng(order)
+        p0 = (base + 0.01 * rng.standard_normal(N)).astype(np.float32)
+        q0 = (0.9 * base).astype(np.float32)
+        _multi_tile_oracle[order] = (wl, P, p0, q0, O.run(P, p0, q0), O.run(P, p0, q0, real=np.float64))
+    return _multi_tile_oracle[order]
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_multi_tile_vs_oracle(semgb_lib, cuda_device, order, kernel):
+    """10 steps from a smooth random state on a box of 0.36-0.52 M nodes that the stencil pass
+    covers with several x- and z-tiles (ragged last tiles) and several y-chunks: every tile and
+    chunk seam is active.  Same tolerance as the fixtures, with the oracle's own FP32 error
+    against FP64 in place of the reference's."""
+    semgb = semgb_lib
+    wl, P, p0, q0, r32, r64 = _multi_tile_case(order)
+    mesh = semgb.Mesh(wl.ex, wl.ey, wl.ez, wl.lx, wl.ly, wl.lz, order)
+    mesh.set_velocity(wl.vel)
+    s = semgb.Solver(mesh, wl.dt)
+    configure(semgb, s, kernel)
+    s.set_sponge_profile(*P.sponge32)
+    s.set_sources(P.src_elem, P.wavelet)
+    s.set_receiver_nodes(P.rec_node)
+    s.set_pressure(semgb.LEVEL_CURRENT, p0)
+    s.set_pressure(semgb.LEVEL_PREVIOUS, q0)
+    s.step(10)
+    p = s.pressure(semgb.LEVEL_CURRENT)
+    tr = s.traces()
+    e_ref_p, e_ref_tr = rel_l2(r32[0], r64[0]), rel_l2(r32[2], r64[2])
+    assert rel_l2(p, r32[0]) <= 1e-5 + 2 * e_ref_p
+    assert rel_l2(p, r64[0]) <= 1e-5 + 1.5 * e_ref_p
+    assert rel_l2(tr, r32[2]) <= 1e-5 + 2 * e_ref_tr
+    assert rel_l2(s.pressure(semgb.LEVEL_PREVIOUS), r32[1]) <= 1e-5
+    s.close()
+    mesh.close()
