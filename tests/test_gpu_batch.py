@@ -22,7 +22,7 @@ def _setup(semgb, order, n_shots, seed):
     return wl, wav
 
 
-@pytest.mark.parametrize("order,n_shots", [(2, 40), (3, 33), (4, 64)])
+@pytest.mark.parametrize("order,n_shots", [(1, 7), (2, 40), (3, 33), (4, 64), (5, 12)])
 def test_batch_matches_plain_solver_per_shot(semgb_lib, cuda_device, order, n_shots):
     semgb = semgb_lib
     wl, wav = _setup(semgb, order, n_shots, seed=50 + order)
