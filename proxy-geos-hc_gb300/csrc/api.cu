@@ -644,11 +644,7 @@ cudaError_t solver_enqueue_step(sem_solver *s, int c, cudaEvent_t *ev, const Ste
         ea.y = s->d_y;
         ea.tab = s->d_tab;
         ea.n_elem = b.n_elem;
-        const int o1 = b.order + 1;
-        for (int i = 0; i < o1; i++) {
-            ea.w[i] = (float)m->gll.w[i];
-            for (int l = 0; l < o1; l++) ea.D[i][l] = (float)m->gll.dphi[l * o1 + i];
-        }
+        element_stiffness_1d(m->gll, ea.S);
         if ((e = launch_element(b.order, ea, s->stream)) != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[2], s->stream);
         UpdateArgs ua{};

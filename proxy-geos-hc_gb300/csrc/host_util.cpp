@@ -91,6 +91,18 @@ void stencil_table(const Gll &g, float *T)
         }
 }
 
+void element_stiffness_1d(const Gll &g, float (&S)[kMaxOrder + 1][kMaxOrder + 1])
+{
+    const int o1 = g.order + 1;
+    for (int i = 0; i <= kMaxOrder; i++)
+        for (int j = 0; j <= kMaxOrder; j++) {
+            double s = 0;
+            if (i < o1 && j < o1)
+                for (int q = 0; q < o1; q++) s += g.w[q] * g.dphi[i * o1 + q] * g.dphi[j * o1 + q];
+            S[i][j] = (float)s;
+        }
+}
+
 float ricker(float time_n, float f0, int order)
 {
     // float/double mix of utils.hpp:11-46, kept so the samples match the reference bit for bit

@@ -26,6 +26,10 @@ bool gll_tables(int order, Gll &g);
 // element, in double, rounded once.
 void stencil_table(const Gll &g, float *T);
 
+// 1-D stiffness of one element, S[i][j] = sum_q w_q phi_i'(xi_q) phi_j'(xi_q) (symmetric), in
+// double, rounded once; rows and columns past the order are zero.
+void element_stiffness_1d(const Gll &g, float (&S)[kMaxOrder + 1][kMaxOrder + 1]);
+
 // Ricker wavelet in the reference's float arithmetic (utils.hpp:11-46).
 float ricker(float t, float f0, int order);
 

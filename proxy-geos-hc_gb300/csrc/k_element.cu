@@ -4,11 +4,13 @@
 // computeMassMatrixAndStiffnessVector (SEMQkGLIntegrals.hpp:206-565).  The reference rebuilds the
 // Jacobian, the mass and a dense (o+1)^3-wide stiffness row per node for every element every step
 // (O(n_pe^2) per element).  Here the mass is precomputed once (launch_mass) and K_e.p is
-// sum-factorised: for each reference direction d,
-//     y_d(i) = sum_l phi_i'(xi_l) * g_d * W(l) * sum_m phi_m'(xi_l) * (p_m - p_l)
-// along the 1-D lines ("pencils") of the element, which is O(n_pe*(o+1)) per element.  The first
-// contraction is written in difference form so that a constant field gives exactly zero (the
-// float-rounded derivative table does not sum exactly to zero per row).
+// sum-factorised: for each reference direction d, along the 1-D lines ("pencils") of the element,
+//     y_d(i) = g_d * W(pencil) * sum_{m != i} S(i, m) * (p_m - p_i)
+// with S the element's 1-D stiffness (S(i, m) = sum_l w_l phi_i'(xi_l) phi_m'(xi_l), the product
+// of the reference's derivative contraction and its transpose, tabulated once in double), which
+// is O(n_pe*(o+1)) per element.  The difference form gives exactly zero on a constant field (the
+// float-rounded rows of S do not sum exactly to zero), and as S is symmetric and
+// p_m - p_i = -(p_i - p_m) exactly, each pair's difference is formed once.
 //
 // CTA shape: TE elements x (o+1)^2 pencils, thread = (pencil, element); TE = 32 (one element per
 // lane, one pencil per warp) for orders 1-4 and 16 for order 5 (36 pencils would exceed 1024
@@ -43,28 +45,25 @@ struct ElemCfg {
                                    sizeof(float) * 3 * NP;
 };
 
-// One direction of the element operator along one pencil: out = D^T (c * (D p)), with the first
-// contraction in difference form.  base = g_d * w_a * w_b of the pencil.
+// One direction of the element operator along one pencil: out = base * S p in difference form,
+// base = g_d * w_a * w_b of the pencil.
 template <int O>
 __device__ __forceinline__ void pencil_apply(const ElementArgs &a, const float (&p)[O + 1],
                                              float base, float (&out)[O + 1])
 {
-    float g[O + 1];
+    float acc[O + 1];
 #pragma unroll
-    for (int l = 0; l <= O; l++) {
-        float u = 0.f;
+    for (int i = 0; i <= O; i++) acc[i] = 0.f;
 #pragma unroll
-        for (int m = 0; m <= O; m++)
-            if (m != l) u = fmaf(a.D[l][m], p[m] - p[l], u);
-        g[l] = (base * a.w[l]) * u;
-    }
+    for (int i = 0; i <= O; i++)
 #pragma unroll
-    for (int i = 0; i <= O; i++) {
-        float acc = 0.f;
+        for (int m = i + 1; m <= O; m++) {
+            const float d = p[m] - p[i];
+            acc[i] = fmaf(a.S[i][m], d, acc[i]);
+            acc[m] = fmaf(-a.S[m][i], d, acc[m]);
+        }
 #pragma unroll
-        for (int l = 0; l <= O; l++) acc = fmaf(a.D[l][i], g[l], acc);
-        out[i] = acc;
-    }
+    for (int i = 0; i <= O; i++) out[i] = base * acc[i];
 }
 
 template <int O>

@@ -33,8 +33,7 @@ struct ElementArgs {
     float *y;            // accumulator
     const float *tab;    // coef table (device)
     int64_t n_elem;
-    float D[6][6];       // D[i][l] = phi_l'(xi_i)
-    float w[6];
+    float S[6][6];       // 1-D element stiffness S[i][m] = sum_l w_l phi_i'(xi_l) phi_m'(xi_l)
 };
 
 struct UpdateArgs {

@@ -165,10 +165,7 @@ extern "C" int sem_element_step_noalloc(int ex, int ey, int ez, float lx, float 
     ea.y = y;
     ea.tab = tab;
     ea.n_elem = b.n_elem;
-    for (int i = 0; i <= order; i++) {
-        ea.w[i] = (float)g.w[i];
-        for (int l = 0; l <= order; l++) ea.D[i][l] = (float)g.dphi[l * (order + 1) + i];
-    }
+    element_stiffness_1d(g, ea.S);
 
     // the array keeps the last call's contents: clear the accumulator this call uses
     cudaError_t e = cudaMemsetAsync(y, 0, b.n_nodes * sizeof(float), s);

@@ -226,6 +226,25 @@ def test_operator_forms_on_a_constant_field(semgb_lib, cuda_device, order):
         s.close()
 
 
+@pytest.mark.parametrize("order", [1, 3, 4, 5])
+def test_element_path_keeps_a_constant_field(semgb_lib, cuda_device, order):
+    """The element path's pencil products are in difference form: a constant field with no source
+    and no sponge stays bit for bit."""
+    from semgb import workloads as W
+    semgb = semgb_lib
+    mesh = semgb.Mesh(6, 5, 4, 60.0, 50.0, 40.0, order)
+    mesh.set_velocity(np.full(6 * 5 * 4, 2000.0, np.float32))
+    const = np.full(mesh.n_nodes, 0.7310585, np.float32)
+    s = semgb.Solver(mesh, W.cfl_dt(10.0, order, 2000.0))
+    s.set_kernel(semgb.KERNEL_ELEMENT)
+    s.set_pressure(semgb.LEVEL_CURRENT, const)
+    s.set_pressure(semgb.LEVEL_PREVIOUS, const)
+    s.step(25)
+    assert np.array_equal(s.pressure(), const)
+    s.close()
+    mesh.close()
+
+
 def test_operator_forms_agree(semgb_lib, cuda_device):
     """The two forms of the stencil pass evaluate the same operator: traces and fields agree to
     FP32 rounding drift over 120 steps."""
