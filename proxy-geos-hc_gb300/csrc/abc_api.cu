@@ -352,7 +352,7 @@ int sem_abc_set_history(sem_abc *a, const float *p_prev)
     if (!a || !p_prev) return sem_fail(SEM_ERR_ARG, "NULL argument");
     const Box &b = a->s->mesh->box;
     CUDA_TRY(cudaStreamSynchronize(a->s->stream));
-    CUDA_TRY(cudaMemcpy2D(a->d_hist, b.nxp * 4, p_prev, b.nx * 4, b.nx * 4, b.nz * b.ny, cudaMemcpyHostToDevice));
+    CUDA_TRY(field_from_host(a->d_hist, p_prev, b.nx, b.nxp, b.nz * b.ny, a->s->stream));
     return SEM_OK;
     GUARD_END
 }

@@ -280,7 +280,7 @@ int sem_adjoint_backward(sem_adjoint *a, const float *residual, float *grad)
     CUDA_TRY(cudaMemcpy(&status, f->d_status, 4, cudaMemcpyDeviceToHost));
     if (status != 0) return sem_fail(SEM_ERR_TIMEOUT, "a bounded wait for a TMA tile gave up in the recompute");
     if (grad)
-        CUDA_TRY(cudaMemcpy2D(grad, b.nx * 4, a->d_grad, b.nxp * 4, b.nx * 4, b.nz * b.ny, cudaMemcpyDeviceToHost));
+        CUDA_TRY(field_to_host(grad, a->d_grad, b.nx, b.nxp, b.nz * b.ny, f->stream));
     return SEM_OK;
     GUARD_END
 }

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <numeric>
 #include <string>
@@ -32,6 +33,94 @@ void solver_invalidate_graphs(sem_solver *s)
     s->graph_gen++;
     for (auto &g : s->graph2)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+namespace {
+
+// Process-wide pinned staging for field_to_host / field_from_host (allocated on first use, kept
+// for the life of the process; calls from several threads take turns).
+struct Staging {
+    static constexpr int64_t kFloats = int64_t(4) << 20;  // 16 MB per buffer
+    std::mutex mu;
+    float *buf[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t init()
+    {
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+            if (!buf[k]) e = cudaHostAlloc(reinterpret_cast<void **>(&buf[k]), kFloats * 4, cudaHostAllocDefault);
+            if (e == cudaSuccess && !ev[k]) e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+        }
+        return e;
+    }
+};
+
+Staging &staging()
+{
+    static Staging st;
+    return st;
+}
+
+}  // namespace
+
+cudaError_t field_to_host(float *dst, const float *src, int64_t nx, int64_t nxp, int64_t rows, cudaStream_t s)
+{
+    Staging &st = staging();
+    std::lock_guard<std::mutex> lock(st.mu);
+    if (nx > Staging::kFloats || st.init() != cudaSuccess) {
+        cudaGetLastError();
+        cudaError_t e = cudaMemcpy2DAsync(dst, nx * 4, src, nxp * 4, nx * 4, rows, cudaMemcpyDeviceToHost, s);
+        return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+    }
+    const int64_t per = Staging::kFloats / nx;  // rows per chunk
+    int64_t prev_r0 = -1, prev_n = 0;
+    int k = 0, prev_k = 0;
+    cudaError_t e = cudaSuccess;
+    for (int64_t r0 = 0; r0 < rows; r0 += per, k ^= 1) {
+        // buffer k was emptied by the host during the previous chunk
+        const int64_t n = std::min(per, rows - r0);
+        if ((e = cudaMemcpy2DAsync(st.buf[k], nx * 4, src + r0 * nxp, nxp * 4, nx * 4, n, cudaMemcpyDeviceToHost,
+                                   s)) != cudaSuccess ||
+            (e = cudaEventRecord(st.ev[k], s)) != cudaSuccess)
+            break;
+        if (prev_r0 >= 0) {
+            if ((e = cudaEventSynchronize(st.ev[prev_k])) != cudaSuccess) break;
+            std::memcpy(dst + prev_r0 * nx, st.buf[prev_k], (size_t)(prev_n * nx) * 4);
+        }
+        prev_r0 = r0; prev_n = n; prev_k = k;
+    }
+    if (e == cudaSuccess && prev_r0 >= 0 && (e = cudaEventSynchronize(st.ev[prev_k])) == cudaSuccess)
+        std::memcpy(dst + prev_r0 * nx, st.buf[prev_k], (size_t)(prev_n * nx) * 4);
+    if (e != cudaSuccess) cudaStreamSynchronize(s);  // leave no copy into the staging in flight
+    return e;
+}
+
+cudaError_t field_from_host(float *dst, const float *src, int64_t nx, int64_t nxp, int64_t rows, cudaStream_t s)
+{
+    Staging &st = staging();
+    std::lock_guard<std::mutex> lock(st.mu);
+    if (nx > Staging::kFloats || st.init() != cudaSuccess) {
+        cudaGetLastError();
+        cudaError_t e = cudaMemcpy2DAsync(dst, nxp * 4, src, nx * 4, nx * 4, rows, cudaMemcpyHostToDevice, s);
+        return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+    }
+    const int64_t per = Staging::kFloats / nx;
+    bool used[2] = {false, false};
+    int k = 0;
+    cudaError_t e = cudaSuccess;
+    for (int64_t r0 = 0; r0 < rows; r0 += per, k ^= 1) {
+        const int64_t n = std::min(per, rows - r0);
+        // the copy that last read buffer k (two chunks ago) must be done before it is refilled
+        if (used[k] && (e = cudaEventSynchronize(st.ev[k])) != cudaSuccess) break;
+        std::memcpy(st.buf[k], src + r0 * nx, (size_t)(n * nx) * 4);
+        if ((e = cudaMemcpy2DAsync(dst + r0 * nxp, nxp * 4, st.buf[k], nx * 4, nx * 4, n, cudaMemcpyHostToDevice,
+                                   s)) != cudaSuccess ||
+            (e = cudaEventRecord(st.ev[k], s)) != cudaSuccess)
+            break;
+        used[k] = true;
+    }
+    const cudaError_t es = cudaStreamSynchronize(s);
+    return e != cudaSuccess ? e : es;
 }
 
 static int resolved_kernel(const sem_solver *s)
@@ -311,8 +400,7 @@ int sem_model_set_node_slowness2(sem_mesh *m, const float *s2)
         CUDA_TRY(dalloc(&m->d_slow2, m->box.n_int));
         CUDA_TRY(cudaMemset(m->d_slow2, 0, m->box.n_int * 4));
     }
-    CUDA_TRY(cudaMemcpy2D(m->d_slow2, m->box.nxp * 4, s2, m->box.nx * 4, m->box.nx * 4,
-                          m->box.nz * m->box.ny, cudaMemcpyHostToDevice));
+    CUDA_TRY(field_from_host(m->d_slow2, s2, m->box.nx, m->box.nxp, m->box.nz * m->box.ny, 0));
     m->model_version++;
     return SEM_OK;
     GUARD_END
@@ -826,7 +914,7 @@ int sem_solver_get_pressure(sem_solver *s, int level, float *out)
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     const int idx = level == SEM_LEVEL_CURRENT ? s->cur : 1 - s->cur;
     // device layout (rows of nxp) -> reference layout (rows of nx)
-    CUDA_TRY(cudaMemcpy2D(out, b.nx * 4, s->d_p[idx], b.nxp * 4, b.nx * 4, b.nz * b.ny, cudaMemcpyDeviceToHost));
+    CUDA_TRY(field_to_host(out, s->d_p[idx], b.nx, b.nxp, b.nz * b.ny, s->stream));
     if (level == SEM_LEVEL_PREVIOUS && s->sponge) {
         // the stored previous level still lacks its last sponge factor
         std::vector<float> sx, sy, sz;
@@ -867,7 +955,7 @@ int sem_solver_set_pressure(sem_solver *s, int level, const float *in)
                     if (f > 0) v[i] = v[i] / f;
                 }
     }
-    CUDA_TRY(cudaMemcpy2D(s->d_p[idx], b.nxp * 4, v.data(), b.nx * 4, b.nx * 4, b.nz * b.ny, cudaMemcpyHostToDevice));
+    CUDA_TRY(field_from_host(s->d_p[idx], v.data(), b.nx, b.nxp, b.nz * b.ny, s->stream));
     return SEM_OK;
     GUARD_END
 }

@@ -71,3 +71,9 @@ void solver_invalidate_graphs(sem_solver *s);
 // Sources by device-layout node with explicit coefficients: p^n[node_k] += coef_k * wavelet_k[n].
 int solver_set_raw_sources(sem_solver *s, int n_src, const int64_t *nodes, const float *coef, const float *wavelet,
                            int n_samples);
+// A field between the device layout (rows of nxp floats) and a host array in the reference
+// layout (rows of nx floats), `rows` rows, through two pinned staging buffers: the copy engine
+// gathers (scatters) one chunk of rows while the host moves the previous one, so the caller's
+// pageable array is not crossed row by row.  Ordered on and synchronous with stream s.
+cudaError_t field_to_host(float *dst, const float *src, int64_t nx, int64_t nxp, int64_t rows, cudaStream_t s);
+cudaError_t field_from_host(float *dst, const float *src, int64_t nx, int64_t nxp, int64_t rows, cudaStream_t s);
