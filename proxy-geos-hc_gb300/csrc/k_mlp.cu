@@ -35,9 +35,11 @@ __device__ __forceinline__ float bf2f(uint16_t u)
     return __bfloat162float(b);
 }
 
+// two floats to BF16 (round to nearest even, as f2bf) in one conversion: lo in the low half
 __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi)
 {
-    return (uint32_t)f2bf(lo) | ((uint32_t)f2bf(hi) << 16);
+    const __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&b);
 }
 
 // GELU in the tanh form of Hendrycks & Gimpel (2016), GELU(z) = z/2 (1 + tanh(u)),
@@ -198,6 +200,90 @@ __device__ void forward_rows(const NetSmem &s, const uint16_t *xs, uint16_t *h1,
                     z2[r * H + c] = za;
                     z2[r * H + c + 1] = zb;
                 }
+                part = fmaf(s.w3[c], gelu(za), part);
+                part = fmaf(s.w3[c + 1], gelu(zb), part);
+            }
+            part += __shfl_xor_sync(0xffffffffu, part, 1);
+            part += __shfl_xor_sync(0xffffffffu, part, 2);
+            yv[mt][hrow] = part + s.b3;
+        }
+}
+
+// As forward_rows for inference (no saved activations), with the hidden layer kept in registers:
+// the m16n8 accumulator fragments of layer-1 columns 16k..16k+15 (n-tiles 2k and 2k+1) are, after
+// bias, GELU and BF16 rounding, exactly the m16n8k16 A fragments of layer 2's k-step k, so no
+// shared-memory copy of the hidden activations is made.  Same roundings and summation order as
+// forward_rows.
+__device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, float (&yv)[2][2])
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    float acc[2][8][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[mt][nt][j] = 0.f;
+#pragma unroll
+    for (int ks = 0; ks < kMlpInPad / 16; ks++) {
+        const int k0 = ks * 16 + q * 2;
+        uint32_t a[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) {
+            const int r = wr + mt * 16 + g;
+            a[mt][0] = *reinterpret_cast<const uint32_t *>(xs + r * KP1 + k0);
+            a[mt][1] = *reinterpret_cast<const uint32_t *>(xs + (r + 8) * KP1 + k0);
+            a[mt][2] = *reinterpret_cast<const uint32_t *>(xs + r * KP1 + k0 + 8);
+            a[mt][3] = *reinterpret_cast<const uint32_t *>(xs + (r + 8) * KP1 + k0 + 8);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            const int n = nt * 8 + g;
+            uint32_t b[2];
+            b[0] = *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0);
+            b[1] = *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0 + 8);
+            mma16816(acc[0][nt], a[0], b);
+            mma16816(acc[1][nt], a[1], b);
+        }
+    }
+    // layer-1 epilogue into layer-2 A fragments: h[mt][ks] = {row g cols 16ks+2q.., row g+8 the
+    // same, row g cols 16ks+8+2q.., row g+8 the same}
+    uint32_t h[2][H / 16][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            const int c = nt * 8 + q * 2;
+#pragma unroll
+            for (int hrow = 0; hrow < 2; hrow++) {
+                const float za = acc[mt][nt][hrow * 2] + s.b1[c], zb = acc[mt][nt][hrow * 2 + 1] + s.b1[c + 1];
+                h[mt][nt >> 1][(nt & 1) * 2 + hrow] = pack_bf2(gelu(za), gelu(zb));
+                acc[mt][nt][hrow * 2] = 0.f;
+                acc[mt][nt][hrow * 2 + 1] = 0.f;
+            }
+        }
+#pragma unroll
+    for (int ks = 0; ks < H / 16; ks++) {
+        const int k0 = ks * 16 + q * 2;
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            const int n = nt * 8 + g;
+            uint32_t b[2];
+            b[0] = *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0);
+            b[1] = *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0 + 8);
+            mma16816(acc[0][nt], h[0][ks], b);
+            mma16816(acc[1][nt], h[1][ks], b);
+        }
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int hrow = 0; hrow < 2; hrow++) {
+            float part = 0.f;
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                const int c = nt * 8 + q * 2;
+                const float za = acc[mt][nt][hrow * 2] + s.b2[c], zb = acc[mt][nt][hrow * 2 + 1] + s.b2[c + 1];
                 part = fmaf(s.w3[c], gelu(za), part);
                 part = fmaf(s.w3[c + 1], gelu(zb), part);
             }
@@ -430,18 +516,26 @@ __global__ void k_mlp_adam(float *p, const float *g, float *m, float *v, float l
 
 // ---- boundary strip ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const AbcArgs a)
+// Four CTAs per SM: the weights, the features and the scales fit 4 x 51 KB of shared memory,
+// the hidden layer stays in registers (forward_rows_regs).  Warp w gathers rows 32w..32w+31 of
+// the tile and runs the network on the same rows, so after the weights are staged the warps
+// only synchronise with themselves.
+// features start on a 16-byte boundary after the weights (their rows are stored 16 bytes at a time)
+constexpr size_t kAbcXsOff = (sizeof(NetSmem) + 15) / 16 * 16;
+static_assert((KP1 * sizeof(uint16_t)) % 16 == 0 && kMlpInPad % 8 == 0, "16-byte feature rows");
+
+__global__ void __launch_bounds__(128, 4) k_abc_correction(const MlpDev net, const AbcArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
-    uint16_t *xs = reinterpret_cast<uint16_t *>(smem + sizeof(NetSmem));
-    uint16_t *h1 = xs + T * KP1;
-    float *scale = reinterpret_cast<float *>(h1 + T * KP2);
+    uint16_t *xs = reinterpret_cast<uint16_t *>(smem + kAbcXsOff);
+    float *scale = reinterpret_cast<float *>(xs + T * KP1);
     load_net(s, net);
+    __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
     const int64_t plane = a.nxp * a.nz;
     for (int64_t row0 = (int64_t)blockIdx.x * T; row0 < a.n; row0 += (int64_t)gridDim.x * T) {
-        __syncthreads();
+        __syncwarp();  // the warp's rows of xs and scale are free again
         // gather, one thread per node: feature (level l, neighbour (dz, dy, dx)) ->
         // l*27 + (dz+1)*9 + (dy+1)*3 + (dx+1); coordinates decoded once, the 27 loads of a level
         // unrolled so that they are in flight together, sponge factors as 3+3+3 axis values.
@@ -488,19 +582,27 @@ __global__ void __launch_bounds__(128) k_abc_correction(const MlpDev net, const 
                 const float sc = m + 1e-30f;
                 scale[r] = sc;
                 const float inv = 1.f / sc;
+                // the row as BF16 pairs (feature k in the low half), zero-padded, stored 8
+                // features at a time (rows are 16-byte aligned)
+                uint32_t pk[kMlpInPad / 2];
 #pragma unroll
-                for (int l = 0; l < 3; l++)
+                for (int k = 0; k < kMlpInPad; k += 2) {
+                    const float lo = k < kMlpIn ? v[k / 27][k % 27] * inv : 0.f;
+                    const float hi = k + 1 < kMlpIn ? v[(k + 1) / 27][(k + 1) % 27] * inv : 0.f;
+                    pk[k / 2] = pack_bf2(lo, hi);
+                }
 #pragma unroll
-                    for (int nb = 0; nb < 27; nb++) xr[l * 27 + nb] = f2bf(v[l][nb] * inv);
-                for (int k = kMlpIn; k < kMlpInPad; k++) xr[k] = 0;
+                for (int c = 0; c < kMlpInPad / 8; c++)
+                    reinterpret_cast<uint4 *>(xr)[c] = make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
             } else {
                 scale[r] = 1e-30f;
-                for (int k = 0; k < kMlpInPad; k++) xr[k] = 0;
+#pragma unroll
+                for (int c = 0; c < kMlpInPad / 8; c++) reinterpret_cast<uint4 *>(xr)[c] = make_uint4(0, 0, 0, 0);
             }
         }
-        __syncthreads();
+        __syncwarp();
         float yv[2][2];
-        forward_rows(s, xs, h1, nullptr, nullptr, w * 32, yv);
+        forward_rows_regs(s, xs, w * 32, yv);
         if (q == 0)
 #pragma unroll
             for (int mt = 0; mt < 2; mt++)
@@ -552,7 +654,7 @@ __global__ void k_gather_rows(const float *x, const float *t, const int64_t *idx
 size_t smem_forward() { return sizeof(NetSmem) + sizeof(uint16_t) * T * (KP1 + KP2); }
 size_t smem_train() { return smem_forward() + sizeof(TrainSmem); }
 size_t smem_w3() { return smem_forward() + sizeof(float) * (T * H + T + H); }
-size_t smem_abc() { return smem_forward() + sizeof(float) * T; }
+size_t smem_abc() { return kAbcXsOff + sizeof(uint16_t) * T * KP1 + sizeof(float) * T; }
 
 int grid_for(int64_t n)
 {
@@ -620,9 +722,9 @@ cudaError_t abc_correction(const MlpDev &net, const AbcArgs &a, cudaStream_t s)
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    // persistent CTAs (three per SM fit the shared memory): the weights are staged once per CTA
+    // persistent CTAs (four per SM fit the shared memory): the weights are staged once per CTA
     const int64_t tiles = (a.n + T - 1) / T;
-    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 152 * 3), T, sm, s>>>(net, a);
+    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 152 * 4), T, sm, s>>>(net, a);
     return cudaGetLastError();
 }
 
