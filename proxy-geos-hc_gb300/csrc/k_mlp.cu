@@ -10,8 +10,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 
 #include "mlp.h"
+#include "tma.cuh"
 
 namespace semgb {
 
@@ -60,6 +62,16 @@ __device__ __forceinline__ float gelu(float z)
     const float t = tanh_hw(gelu_u(z));
     const float h = 0.5f * z;
     return fmaf(h, t, h);
+}
+// gelu of two values with packed f32x2 arithmetic: the same operations in the same order as gelu,
+// each half rounded as the scalar instruction would round it
+__device__ __forceinline__ float2 gelu2(float2 z)
+{
+    const float2 w = fma2(make_float2(kGeluCA, kGeluCA), mul2(z, z), make_float2(kGeluC, kGeluC));
+    const float2 u = mul2(z, w);
+    const float2 t = make_float2(tanh_hw(u.x), tanh_hw(u.y));
+    const float2 h = mul2(make_float2(0.5f, 0.5f), z);
+    return fma2(h, t, h);
 }
 __device__ __forceinline__ float gelu_d(float z)
 {
@@ -256,8 +268,10 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
             const int c = nt * 8 + q * 2;
 #pragma unroll
             for (int hrow = 0; hrow < 2; hrow++) {
-                const float za = acc[mt][nt][hrow * 2] + s.b1[c], zb = acc[mt][nt][hrow * 2 + 1] + s.b1[c + 1];
-                h[mt][nt >> 1][(nt & 1) * 2 + hrow] = pack_bf2(gelu(za), gelu(zb));
+                const float2 z = add2(make_float2(acc[mt][nt][hrow * 2], acc[mt][nt][hrow * 2 + 1]),
+                                      *reinterpret_cast<const float2 *>(s.b1 + c));
+                const float2 gz = gelu2(z);
+                h[mt][nt >> 1][(nt & 1) * 2 + hrow] = pack_bf2(gz.x, gz.y);
                 acc[mt][nt][hrow * 2] = 0.f;
                 acc[mt][nt][hrow * 2 + 1] = 0.f;
             }
@@ -283,9 +297,11 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
 #pragma unroll
             for (int nt = 0; nt < 8; nt++) {
                 const int c = nt * 8 + q * 2;
-                const float za = acc[mt][nt][hrow * 2] + s.b2[c], zb = acc[mt][nt][hrow * 2 + 1] + s.b2[c + 1];
-                part = fmaf(s.w3[c], gelu(za), part);
-                part = fmaf(s.w3[c + 1], gelu(zb), part);
+                const float2 z = add2(make_float2(acc[mt][nt][hrow * 2], acc[mt][nt][hrow * 2 + 1]),
+                                      *reinterpret_cast<const float2 *>(s.b2 + c));
+                const float2 gz = gelu2(z);
+                part = fmaf(s.w3[c], gz.x, part);
+                part = fmaf(s.w3[c + 1], gz.y, part);
             }
             part += __shfl_xor_sync(0xffffffffu, part, 1);
             part += __shfl_xor_sync(0xffffffffu, part, 2);
@@ -520,6 +536,7 @@ __global__ void k_mlp_adam(float *p, const float *g, float *m, float *v, float l
 // the hidden layer stays in registers (forward_rows_regs).  Warp w gathers rows 32w..32w+31 of
 // the tile and runs the network on the same rows, so after the weights are staged the warps
 // only synchronise with themselves.
+static_assert(offsetof(NetSmem, b1) % 8 == 0 && offsetof(NetSmem, b2) % 8 == 0, "bias pairs load as float2");
 // features start on a 16-byte boundary after the weights (their rows are stored 16 bytes at a time)
 constexpr size_t kAbcXsOff = (sizeof(NetSmem) + 15) / 16 * 16;
 static_assert((KP1 * sizeof(uint16_t)) % 16 == 0 && kMlpInPad % 8 == 0, "16-byte feature rows");
@@ -587,9 +604,13 @@ __global__ void __launch_bounds__(128, 4) k_abc_correction(const MlpDev net, con
                 uint32_t pk[kMlpInPad / 2];
 #pragma unroll
                 for (int k = 0; k < kMlpInPad; k += 2) {
-                    const float lo = k < kMlpIn ? v[k / 27][k % 27] * inv : 0.f;
-                    const float hi = k + 1 < kMlpIn ? v[(k + 1) / 27][(k + 1) % 27] * inv : 0.f;
-                    pk[k / 2] = pack_bf2(lo, hi);
+                    if (k < kMlpIn) {
+                        const float2 f = mul2(make_float2(v[k / 27][k % 27], k + 1 < kMlpIn ? v[(k + 1) / 27][(k + 1) % 27] : 0.f),
+                                              make_float2(inv, inv));
+                        pk[k / 2] = pack_bf2(f.x, f.y);
+                    } else {
+                        pk[k / 2] = 0u;
+                    }
                 }
 #pragma unroll
                 for (int c = 0; c < kMlpInPad / 8; c++)

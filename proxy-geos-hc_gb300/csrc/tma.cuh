@@ -97,6 +97,13 @@ __device__ __forceinline__ float2 unpack2(unsigned long long r)
     return a;
 }
 
+__device__ __forceinline__ float2 add2(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+
 __device__ __forceinline__ float2 sub2(float2 a, float2 b)
 {
     unsigned long long r;
