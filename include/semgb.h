@@ -11,7 +11,10 @@
  *    crosses this boundary.
  *  - The library owns all device memory.  Buffers passed in or out are host memory owned by the
  *    caller unless a name says "device".  Functions that return data synchronise the solver's
- *    stream first; sem_solver_step only enqueues work.
+ *    stream first; sem_solver_step only enqueues work.  Whole fields (pressure levels, squared
+ *    slowness, gradients) cross through the library's pinned staging buffers, so the caller's
+ *    arrays may be ordinary pageable memory; the first such copy in a process pins 32 MB of host
+ *    memory, kept until the process exits.
  *  - A handle is used by one host thread at a time; separate solvers may run on separate streams.
  *  - Node numbering is the reference's: node = ix + iz*nx + iy*nx*nz with nx = ex*order+1 etc.
  *    (SEMmesh.cpp:142-231); element e = ix + iz*ex + iy*ex*ez; coordinates are (x, y, z).
