@@ -41,6 +41,9 @@ namespace {
 #ifndef SEM_STENCIL_NG
 #define SEM_STENCIL_NG 2  // row groups per thread where the order allows it
 #endif
+#ifndef SEM_STENCIL_PACKED
+#define SEM_STENCIL_PACKED 1  // even orders: the per-node update in packed f32x2 arithmetic
+#endif
 #ifndef SEM_STENCIL_RW
 #define SEM_STENCIL_RW 2  // rows per warp instruction where the order allows it
 #endif
@@ -434,17 +437,44 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
             const float gx = t.g[0] * (wz * wy), gzy = t.g[1] * wy, gyz = t.g[2] * wz;
             float *dst = dst_col + (int64_t)y * plane_stride;
             float out[NG][O], kp[NG][O], sv[NG][O], qdv[NG][O];
+            if constexpr (SEM_STENCIL_PACKED && O % 2 == 0) {
+                // node pairs in packed f32x2: the same operations in the same order as the
+                // scalar form below, each half rounded as the scalar instruction
 #pragma unroll
-            for (int g = 0; g < NG; g++) {
+                for (int g = 0; g < NG; g++) {
 #pragma unroll
-                for (int j = 0; j < O; j++) {
-                    const float wxj = c_wa[O - 1][j];
-                    sv[g][j] = SPONGE ? sxz[g][j] * syv : 1.f;
-                    qdv[g][j] = SPONGE ? sv[g][j] * q[g][j] : q[g][j];
-                    // K.p at the node: g1 Wz Wy A_x + Wx (g2 Wy A_z + g3 Wz A_y)
-                    const float yv = fmaf(wxj, fmaf(gyz, ay.v[g][j], gzy * az.v[g][j]), gx * ax[g][j]);
-                    out[g][j] = (2.f * c[g][j] - qdv[g][j]) - am[g][j] * yv;
-                    if (MODE == STENCIL_RECORD_KP) kp[g][j] = yv;
+                    for (int j = 0; j < O; j += 2) {
+                        const float2 s2 = SPONGE ? mul2(make_float2(sxz[g][j], sxz[g][j + 1]), make_float2(syv, syv))
+                                                 : make_float2(1.f, 1.f);
+                        const float2 q2 = make_float2(q[g][j], q[g][j + 1]);
+                        const float2 qd2 = SPONGE ? mul2(s2, q2) : q2;
+                        const float2 y2 =
+                            fma2(make_float2(c_wa[O - 1][j], c_wa[O - 1][j + 1]),
+                                 fma2(make_float2(gyz, gyz), make_float2(ay.v[g][j], ay.v[g][j + 1]),
+                                      mul2(make_float2(gzy, gzy), make_float2(az.v[g][j], az.v[g][j + 1]))),
+                                 mul2(make_float2(gx, gx), make_float2(ax[g][j], ax[g][j + 1])));
+                        // (2c - qd) - am*y: 2c is exact, then one fused multiply-add
+                        const float2 t2 = sub2(mul2(make_float2(2.f, 2.f), make_float2(c[g][j], c[g][j + 1])), qd2);
+                        const float2 o2 = fma2(make_float2(-am[g][j], -am[g][j + 1]), y2, t2);
+                        sv[g][j] = s2.x; sv[g][j + 1] = s2.y;
+                        qdv[g][j] = qd2.x; qdv[g][j + 1] = qd2.y;
+                        out[g][j] = o2.x; out[g][j + 1] = o2.y;
+                        if (MODE == STENCIL_RECORD_KP) { kp[g][j] = y2.x; kp[g][j + 1] = y2.y; }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int g = 0; g < NG; g++) {
+#pragma unroll
+                    for (int j = 0; j < O; j++) {
+                        const float wxj = c_wa[O - 1][j];
+                        sv[g][j] = SPONGE ? sxz[g][j] * syv : 1.f;
+                        qdv[g][j] = SPONGE ? sv[g][j] * q[g][j] : q[g][j];
+                        // K.p at the node: g1 Wz Wy A_x + Wx (g2 Wy A_z + g3 Wz A_y)
+                        const float yv = fmaf(wxj, fmaf(gyz, ay.v[g][j], gzy * az.v[g][j]), gx * ax[g][j]);
+                        out[g][j] = (2.f * c[g][j] - qdv[g][j]) - am[g][j] * yv;
+                        if (MODE == STENCIL_RECORD_KP) kp[g][j] = yv;
+                    }
                 }
             }
             if (!(inner && yin)) {
