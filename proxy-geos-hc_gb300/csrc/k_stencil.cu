@@ -42,7 +42,7 @@ namespace {
 #define SEM_STENCIL_NG 2  // row groups per thread where the order allows it
 #endif
 #ifndef SEM_STENCIL_PACKED
-#define SEM_STENCIL_PACKED 1  // even orders: the per-node update in packed f32x2 arithmetic
+#define SEM_STENCIL_PACKED 1  // the per-node update of node pairs in packed f32x2 arithmetic
 #endif
 #ifndef SEM_STENCIL_RW
 #define SEM_STENCIL_RW 2  // rows per warp instruction where the order allows it
@@ -437,13 +437,14 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
             const float gx = t.g[0] * (wz * wy), gzy = t.g[1] * wy, gyz = t.g[2] * wz;
             float *dst = dst_col + (int64_t)y * plane_stride;
             float out[NG][O], kp[NG][O], sv[NG][O], qdv[NG][O];
-            if constexpr (SEM_STENCIL_PACKED && O % 2 == 0) {
+            if constexpr (SEM_STENCIL_PACKED && O > 1) {
                 // node pairs in packed f32x2: the same operations in the same order as the
-                // scalar form below, each half rounded as the scalar instruction
+                // scalar form below, each half rounded as the scalar instruction; an odd order's
+                // last node of the run alone
 #pragma unroll
                 for (int g = 0; g < NG; g++) {
 #pragma unroll
-                    for (int j = 0; j < O; j += 2) {
+                    for (int j = 0; j + 1 < O; j += 2) {
                         const float2 s2 = SPONGE ? mul2(make_float2(sxz[g][j], sxz[g][j + 1]), make_float2(syv, syv))
                                                  : make_float2(1.f, 1.f);
                         const float2 q2 = make_float2(q[g][j], q[g][j + 1]);
@@ -460,6 +461,14 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
                         qdv[g][j] = qd2.x; qdv[g][j + 1] = qd2.y;
                         out[g][j] = o2.x; out[g][j + 1] = o2.y;
                         if (MODE == STENCIL_RECORD_KP) { kp[g][j] = y2.x; kp[g][j + 1] = y2.y; }
+                    }
+                    if constexpr (O % 2 == 1) {
+                        constexpr int j = O - 1;
+                        sv[g][j] = SPONGE ? sxz[g][j] * syv : 1.f;
+                        qdv[g][j] = SPONGE ? sv[g][j] * q[g][j] : q[g][j];
+                        const float yv = fmaf(c_wa[O - 1][j], fmaf(gyz, ay.v[g][j], gzy * az.v[g][j]), gx * ax[g][j]);
+                        out[g][j] = (2.f * c[g][j] - qdv[g][j]) - am[g][j] * yv;
+                        if (MODE == STENCIL_RECORD_KP) kp[g][j] = yv;
                     }
                 }
             } else {
