@@ -44,6 +44,9 @@ namespace {
 #ifndef SEM_STENCIL_PACKED
 #define SEM_STENCIL_PACKED 1  // the per-node update of node pairs in packed f32x2 arithmetic
 #endif
+#ifndef SEM_STENCIL_PACKED_AXIS
+#define SEM_STENCIL_PACKED_AXIS 1  // even orders, direct form: z- and y-terms on packed node pairs
+#endif
 #ifndef SEM_STENCIL_RW
 #define SEM_STENCIL_RW 2  // rows per warp instruction where the order allows it
 #endif
@@ -55,6 +58,7 @@ constexpr int kL2Pf = SEM_STENCIL_L2PF;       // further planes prefetched into 
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 constexpr int kTMax = kMaxOrder * (2 * kMaxOrder + 1);
 __constant__ float c_T[kMaxOrder][kTMax];  // [order-1][l * (2o+1) + d + o]
+__constant__ float2 c_T2[kMaxOrder][kTMax];  // the same coefficients twice, for packed node pairs
 __constant__ float c_wa[kMaxOrder][kMaxOrder];  // assembled weights by local index
 
 template <int O>
@@ -160,7 +164,36 @@ template <int O, int NG, int GS, int LOC, bool DIRECT, class RowFn>
 __device__ __forceinline__ VecG<O, NG> axis_uniform(const float (&c)[NG][O], const RowFn &row)
 {
     VecG<O, NG> r;
-    if constexpr (DIRECT) {
+    if constexpr (DIRECT && SEM_STENCIL_PACKED_AXIS && O % 2 == 0) {
+        // node pairs in packed f32x2 with the coefficient pair from the constant bank: the same
+        // products and sums in the same order as the scalar form below, each half rounded alike
+        float2 rr[NG][O / 2];
+        const float2 td = c_T2[O - 1][LOC * (2 * O + 1) + O];
+#pragma unroll
+        for (int g = 0; g < NG; g++)
+#pragma unroll
+            for (int jp = 0; jp < O / 2; jp++) rr[g][jp] = mul2(td, make_float2(c[g][2 * jp], c[g][2 * jp + 1]));
+#pragma unroll
+        for (int d = dlo(O, LOC); d <= dhi(O, LOC); d++) {
+            if (d == 0) continue;
+            const float *p = row(d);
+            const float2 tt = c_T2[O - 1][LOC * (2 * O + 1) + d + O];
+#pragma unroll
+            for (int g = 0; g < NG; g++) {
+                float v[O];
+                load_o<O>(p + g * GS, v);
+#pragma unroll
+                for (int jp = 0; jp < O / 2; jp++) rr[g][jp] = fma2(tt, make_float2(v[2 * jp], v[2 * jp + 1]), rr[g][jp]);
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < NG; g++)
+#pragma unroll
+            for (int jp = 0; jp < O / 2; jp++) {
+                r.v[g][2 * jp] = rr[g][jp].x;
+                r.v[g][2 * jp + 1] = rr[g][jp].y;
+            }
+    } else if constexpr (DIRECT) {
         // the coefficients are constant-bank operands of scalar fmas
 #pragma unroll
         for (int g = 0; g < NG; g++)
@@ -839,6 +872,9 @@ cudaError_t stencil_kernel_setup()
         for (int l = 0; l < o; l++) wa[(o - 1) * kMaxOrder + l] = (float)(l == 0 ? g.w[0] + g.w[o] : g.w[l]);
     }
     if ((e = cudaMemcpyToSymbol(c_T, all.data(), all.size() * sizeof(float))) != cudaSuccess) return e;
+    std::vector<float2> all2(all.size());
+    for (size_t i = 0; i < all.size(); i++) all2[i] = make_float2(all[i], all[i]);
+    if ((e = cudaMemcpyToSymbol(c_T2, all2.data(), all2.size() * sizeof(float2))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(c_wa, wa.data(), wa.size() * sizeof(float))) != cudaSuccess) return e;
     if ((e = setup_o<1>()) != cudaSuccess) return e;
     if ((e = setup_o<2>()) != cudaSuccess) return e;
