@@ -33,8 +33,10 @@ namespace semgb {
 
 namespace {
 
-// Tiling knobs (compile-time; the defaults are the measured best on GB300, other values are
-// for sweeps: build.py -D NAME=value builds a separate library).
+// Tiling and arithmetic knobs (compile-time; the defaults are the measured best on GB300, other
+// values are for sweeps: build.py -D NAME=value builds a separate library).  Both settings of the
+// two packing knobs give the same bits: a packed f32x2 instruction rounds each half as the scalar
+// instruction does.
 #ifndef SEM_STENCIL_LOOKAHEAD
 #define SEM_STENCIL_LOOKAHEAD 1  // planes loaded into shared memory ahead of the compute
 #endif
