@@ -56,6 +56,18 @@ enum {
    L2 in the traces), ~5 % slower. */
 enum { SEM_FORM_DIRECT = 0, SEM_FORM_DIFFERENCE = 1 };
 
+/* Rounding of the stiffness operator (sem_solver_set_rounding).
+   DEFAULT: the operator as the build forms it (tensor-product coefficients for the stencil pass,
+   the element's 1-D stiffness in difference form for the element pass).
+   REFERENCE: the reference's own float-rounded element rows (sem_box_refround_rows), so that
+   the FP32 result follows the reference's rather than drifting from it by the two codes' FP32
+   errors: the stencil pass steps with their assembled node-class coefficients
+   (sem_box_refround_class_table), one accumulation per node; the element pass applies the rows
+   pencil by pencil.  On the 40^3 Q2 1500-step workload the two stay within 1.2e-6 (traces) and
+   6.5e-6 (final pressure) relative L2 of the compiled reference, against 2.1e-4 and 4.1e-3 in
+   DEFAULT. */
+enum { SEM_ROUNDING_DEFAULT = 0, SEM_ROUNDING_REFERENCE = 1 };
+
 /* Pressure levels for sem_solver_get_pressure / sem_solver_set_pressure. */
 enum { SEM_LEVEL_CURRENT = 0, SEM_LEVEL_PREVIOUS = 1 };
 
@@ -112,6 +124,24 @@ int sem_box_nearest_node(int ex, int ey, int ez, float lx, float ly, float lz, i
 int sem_box_sponge_profile(int ex, int ey, int ez, float lx, float ly, float lz, int order,
                            int thickness, float sigma, float *sx, float *sy, float *sz);
 
+/* The reference's element stiffness rows on one element of the box, rounded as the reference
+ * rounds them: computeB's metric in double stored as float, each entry of gradPhiGradPhi's row
+ * accumulated in float from double products in its loop order (SEMQkGLIntegrals.hpp:265-513).
+ * The box's elements are axis-aligned, so the row of node i has its non-zero entries on the three
+ * coordinate lines through i.  rows[3*(order+1)^3*(order+1)]: rows[(a*npe + i)*(order+1) + m] is
+ * the entry of node i (local numbering) toward the node of local index m along axis a (0: x,
+ * 1: z, 2: y); the x entry at i's own index holds the whole diagonal, the z and y ones zero.
+ * These are the rows SEM_ROUNDING_REFERENCE steps with. */
+int sem_box_refround_rows(int ex, int ey, int ez, float lx, float ly, float lz, int order, float *rows);
+
+/* Node-class coefficients of the operator the reference assembles from those rows: for a node
+ * with local indices (lx, lz, ly) in 0..order-1, the coefficient of the node d places along axis
+ * a, summed exactly over the elements holding both nodes and rounded once; the diagonal is the x
+ * entry at d = 0.  tab[3*order*order*(2*order+1)*order], index (((a*o + ly)*o + lz)*(2o+1) + d +
+ * o)*o + lx.  The stencil pass steps with this table under SEM_ROUNDING_REFERENCE. */
+int sem_box_refround_class_table(int ex, int ey, int ez, float lx, float ly, float lz, int order,
+                                 float *tab);
+
 /* ------------------------------------------------------------------------------------------
  * Mesh and model (device).
  * ------------------------------------------------------------------------------------------ */
@@ -160,6 +190,12 @@ int sem_solver_set_kernel(sem_solver *s, int kernel);
 /* Operator form of the stencil kernel (SEM_FORM_*; default SEM_FORM_DIRECT).  The element kernel
    always uses the difference form.  Extension: the reference has one form. */
 int sem_solver_set_operator_form(sem_solver *s, int form);
+
+/* Rounding of the stiffness operator (SEM_ROUNDING_*; default SEM_ROUNDING_DEFAULT).  The
+   reference's rows are built for the mesh's exact element size; they are the reference's own
+   bit for bit where its float node coordinates are exact (orders 1 and 2 with integer element
+   sizes).  SEM_ROUNDING_REFERENCE ignores the operator form.  Extension: parity mode. */
+int sem_solver_set_rounding(sem_solver *s, int rounding);
 
 /* Sponge of `thickness` elements with boundary damping sigma (0 thickness: none), or explicit
  * per-axis factors (see sem_box_sponge_profile).  Applied after each step to both levels. */

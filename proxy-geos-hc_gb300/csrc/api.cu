@@ -293,6 +293,34 @@ int sem_box_sponge_profile(int ex, int ey, int ez, float lx, float ly, float lz,
     GUARD_END
 }
 
+int sem_box_refround_rows(int ex, int ey, int ez, float lx, float ly, float lz, int order, float *rows)
+{
+    GUARD_BEGIN
+    Box b;
+    Gll g;
+    if (!make_box(ex, ey, ez, lx, ly, lz, order, b) || !gll_tables(order, g) || !rows)
+        return fail(SEM_ERR_ARG, "bad box");
+    std::vector<float> r;
+    reference_element_rows(g, 0.5 * lx / ex, 0.5 * lz / ez, 0.5 * ly / ey, r);
+    std::copy(r.begin(), r.end(), rows);
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_box_refround_class_table(int ex, int ey, int ez, float lx, float ly, float lz, int order, float *tab)
+{
+    GUARD_BEGIN
+    Box b;
+    Gll g;
+    if (!make_box(ex, ey, ez, lx, ly, lz, order, b) || !gll_tables(order, g) || !tab)
+        return fail(SEM_ERR_ARG, "bad box");
+    std::vector<float> t;
+    reference_class_table(g, 0.5 * lx / ex, 0.5 * lz / ez, 0.5 * ly / ey, t);
+    std::copy(t.begin(), t.end(), tab);
+    return SEM_OK;
+    GUARD_END
+}
+
 // ----------------------------------------------------------------------------------------------
 // mesh and model
 // ----------------------------------------------------------------------------------------------
@@ -419,6 +447,8 @@ int sem_solver_destroy(sem_solver *s)
     dfree(s->d_y);
     dfree(s->d_a);
     dfree(s->d_tab);
+    dfree(s->d_rtab);
+    dfree(s->d_mref);
     dfree(s->d_w);
     stencil_tables_free(s->stencil);
     dfree(s->d_sx);
@@ -522,6 +552,18 @@ int sem_solver_set_operator_form(sem_solver *s, int form)
         cudaStreamSynchronize(s->stream);
         solver_invalidate_graphs(s);
         s->form = form;
+    }
+    return SEM_OK;
+}
+
+int sem_solver_set_rounding(sem_solver *s, int rounding)
+{
+    if (!s) return fail(SEM_ERR_ARG, "NULL solver");
+    if (rounding != SEM_ROUNDING_DEFAULT && rounding != SEM_ROUNDING_REFERENCE) return fail(SEM_ERR_ARG, "unknown rounding");
+    if (rounding != s->rounding) {
+        cudaStreamSynchronize(s->stream);
+        solver_invalidate_graphs(s);
+        s->rounding = rounding;
     }
     return SEM_OK;
 }
@@ -669,6 +711,25 @@ int solver_prepare(sem_solver *s, int64_t n_new)
             CUDA_TRY(dalloc(&s->d_y, s->n_int));
             CUDA_TRY(cudaMemsetAsync(s->d_y, 0, s->n_int * 4, s->stream));
         }
+        if (s->rounding == SEM_ROUNDING_REFERENCE && !s->d_rtab) {
+            const Box &b = m->box;
+            std::vector<float> rows;
+            reference_element_rows(m->gll, 0.5 * b.lx / b.ex, 0.5 * b.lz / b.ez, 0.5 * b.ly / b.ey, rows);
+            CUDA_TRY(dalloc(&s->d_rtab, rows.size()));
+            CUDA_TRY(cudaMemcpy(s->d_rtab, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
+            solver_invalidate_graphs(s);
+        }
+        if (s->rounding == SEM_ROUNDING_REFERENCE && !m->d_slow2 && s->mref_version != m->model_version) {
+            const Box &b = m->box;
+            if (!s->d_mref) {
+                CUDA_TRY(dalloc(&s->d_mref, s->n_int));
+                solver_invalidate_graphs(s);
+            }
+            // detJ grouped as computeB forms it (SEMQkGLIntegrals.hpp:316-318)
+            const double detJ = std::fabs((0.5 * b.lx / b.ex) * ((0.5 * b.lz / b.ez) * (0.5 * b.ly / b.ey)));
+            CUDA_TRY(launch_mass_ref(s->d_mref, m->d_vel, b.ex, b.ey, b.ez, b.order, b.nxp, s->d_w, detJ, s->stream));
+            s->mref_version = m->model_version;
+        }
         if (s->upd_rec_version != s->rec_version) {
             dfree(s->d_upd_rec_off);
             if (s->nrec > 0) {
@@ -686,6 +747,14 @@ int solver_prepare(sem_solver *s, int64_t n_new)
         if (!s->stencil) {
             int rc = stencil_tables_create(m->box, m->gll, m->geo, 1, &s->stencil);
             if (rc) return fail(SEM_ERR_CUDA, "stencil tables");
+        }
+        const bool want_class = s->rounding == SEM_ROUNDING_REFERENCE;
+        if (want_class != (s->stencil->class_tab != nullptr)) {
+            std::vector<float> tab;
+            const Box &b = m->box;
+            if (want_class) reference_class_table(m->gll, 0.5 * b.lx / b.ex, 0.5 * b.lz / b.ez, 0.5 * b.ly / b.ey, tab);
+            stencil_set_class_table(*s->stencil, want_class ? tab.data() : nullptr);
+            solver_invalidate_graphs(s);
         }
         if (stencil_bind(*s->stencil, s->d_p[0], s->d_p[1], s->d_a) != 0)
             return fail(SEM_ERR_CUDA, "tensor-map encoding failed (driver entry point cuTensorMapEncodeTiled)");
@@ -731,6 +800,7 @@ cudaError_t solver_enqueue_step(sem_solver *s, int c, cudaEvent_t *ev, const Ste
         ea.p = s->d_p[c];
         ea.y = s->d_y;
         ea.tab = s->d_tab;
+        ea.rtab = s->rounding == SEM_ROUNDING_REFERENCE ? s->d_rtab : nullptr;
         ea.n_elem = b.n_elem;
         element_stiffness_1d(m->gll, ea.S);
         if ((e = launch_element(b.order, ea, s->stream)) != cudaSuccess) return e;
@@ -748,6 +818,10 @@ cudaError_t solver_enqueue_step(sem_solver *s, int c, cudaEvent_t *ev, const Ste
         ua.nrec = s->nrec;
         ua.traces = s->d_traces;
         ua.ctr = s->d_ctr;
+        if (s->rounding == SEM_ROUNDING_REFERENCE && !m->d_slow2) {
+            ua.mref = s->d_mref;
+            ua.dt2f = s->dt * s->dt;  // rounded as the reference's myTimeStep*myTimeStep
+        }
         if ((e = launch_update(ua, s->sponge, s->stream)) != cudaSuccess) return e;
     } else {
         StencilArgs ta{};
@@ -768,7 +842,7 @@ cudaError_t solver_enqueue_step(sem_solver *s, int c, cudaEvent_t *ev, const Ste
             ta.kp = extra->kp;
             ta.grad = extra->grad;
         }
-        const bool direct = s->form == SEM_FORM_DIRECT;
+        const bool direct = s->form == SEM_FORM_DIRECT || s->rounding == SEM_ROUNDING_REFERENCE;
         if ((e = launch_stencil(*s->stencil, ta, c, s->sponge, s->stream, mode, direct)) != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[2], s->stream);
     }

@@ -103,6 +103,85 @@ void element_stiffness_1d(const Gll &g, float (&S)[kMaxOrder + 1][kMaxOrder + 1]
         }
 }
 
+void reference_element_rows(const Gll &g, double jx, double jz, double jy, std::vector<float> &rows)
+{
+    const int o = g.order, o1 = o + 1, op2 = o1 * o1, npe = op2 * o1;
+    const double *w = g.w;
+    auto D = [&](int a, int b) { return g.dphi[a * o1 + b]; };  // phi_a'(xi_b)
+    // computeB (SEMQkGLIntegrals.hpp:316-349) with jac = diag(jx, jz, jy): the cofactors off the
+    // diagonal vanish, detJ = |jx (jz jy)|, B_dd = adj_dd^2 / detJ; the same at every GLL point
+    const double detJ = std::fabs(jx * (jz * jy));
+    const double a00 = jz * jy, a11 = jx * jy, a22 = jx * jz;
+    const double dm1 = 1. / detJ;
+    const float B[3] = {(float)((a00 * a00) * dm1), (float)((a11 * a11) * dm1), (float)((a22 * a22) * dm1)};
+    rows.assign((size_t)3 * npe * o1, 0.f);
+    std::vector<float> R(npe);
+    // gradPhiGradPhi (SEMQkGLIntegrals.hpp:427-513): the three line families in the reference's
+    // order; the cross families add exact zeros here
+    for (int i3 = 0; i3 < o1; i3++)
+        for (int i2 = 0; i2 < o1; i2++)
+            for (int i1 = 0; i1 < o1; i1++) {
+                std::fill(R.begin(), R.end(), 0.f);
+                for (int j1 = 0; j1 < o1; j1++) {
+                    const int j = j1 + i2 * o1 + i3 * op2;
+                    for (int l = 0; l < o1; l++)
+                        R[j] = (float)((double)R[j] + w[l] * w[i2] * w[i3] * ((double)B[0] * D(i1, l) * D(j1, l)));
+                }
+                for (int j2 = 0; j2 < o1; j2++) {
+                    const int j = i1 + j2 * o1 + i3 * op2;
+                    for (int m = 0; m < o1; m++)
+                        R[j] = (float)((double)R[j] + w[i1] * w[m] * w[i3] * ((double)B[1] * D(i2, m) * D(j2, m)));
+                }
+                for (int j3 = 0; j3 < o1; j3++) {
+                    const int j = i1 + i2 * o1 + j3 * op2;
+                    for (int n = 0; n < o1; n++)
+                        R[j] = (float)((double)R[j] + w[i1] * w[i2] * w[n] * ((double)B[2] * D(i3, n) * D(j3, n)));
+                }
+                const int i = i1 + i2 * o1 + i3 * op2;
+                for (int m = 0; m < o1; m++) {
+                    rows[((size_t)0 * npe + i) * o1 + m] = R[m + i2 * o1 + i3 * op2];
+                    if (m != i2) rows[((size_t)1 * npe + i) * o1 + m] = R[i1 + m * o1 + i3 * op2];
+                    if (m != i3) rows[((size_t)2 * npe + i) * o1 + m] = R[i1 + i2 * o1 + m * op2];
+                }
+            }
+}
+
+void reference_class_table(const Gll &g, double jx, double jz, double jy, std::vector<float> &tab)
+{
+    const int o = g.order, o1 = o + 1, npe = o1 * o1 * o1, W = 2 * o + 1;
+    std::vector<float> rows;
+    reference_element_rows(g, jx, jz, jy, rows);
+    tab.assign((size_t)reference_class_table_size(o), 0.f);
+    // the elements holding a node of local index l along an axis: l itself, and for l = 0 also
+    // the element before it, where the node has local index o
+    auto members = [o](int l, int *loc) {
+        loc[0] = l;
+        if (l != 0) return 1;
+        loc[1] = o;
+        return 2;
+    };
+    for (int ly = 0; ly < o; ly++)
+        for (int lz = 0; lz < o; lz++)
+            for (int lx = 0; lx < o; lx++) {
+                double acc[3][2 * kMaxOrder + 1] = {};
+                int mx[2], mz[2], my[2];
+                const int nx = members(lx, mx), nz = members(lz, mz), ny = members(ly, my);
+                for (int a = 0; a < nx; a++)
+                    for (int b = 0; b < nz; b++)
+                        for (int c = 0; c < ny; c++) {
+                            const int ix = mx[a], iz = mz[b], iy = my[c];
+                            const int i = ix + iz * o1 + iy * o1 * o1;
+                            const int own[3] = {ix, iz, iy};
+                            for (int ax = 0; ax < 3; ax++)
+                                for (int m = 0; m < o1; m++)
+                                    acc[ax][m - own[ax] + o] += rows[((size_t)ax * npe + i) * o1 + m];
+                        }
+                for (int ax = 0; ax < 3; ax++)
+                    for (int d = -o; d <= o; d++)
+                        tab[((((size_t)ax * o + ly) * o + lz) * W + d + o) * o + lx] = (float)acc[ax][d + o];
+            }
+}
+
 float ricker(float time_n, float f0, int order)
 {
     // float/double mix of utils.hpp:11-46, kept so the samples match the reference bit for bit

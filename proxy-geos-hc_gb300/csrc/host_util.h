@@ -30,6 +30,25 @@ void stencil_table(const Gll &g, float *T);
 // double, rounded once; rows and columns past the order are zero.
 void element_stiffness_1d(const Gll &g, float (&S)[kMaxOrder + 1][kMaxOrder + 1]);
 
+// The reference's element stiffness rows (computeB and gradPhiGradPhi, SEMQkGLIntegrals.hpp:265-
+// 513) on an axis-aligned element with Jacobian diag(jx, jz, jy) (reference directions xi1 -> x,
+// xi2 -> z, xi3 -> y), rounded where the reference rounds: the metric B computed in double and
+// stored as float, every row entry accumulated in float from double products in the reference's
+// loop order.  The off-diagonal metric terms are exactly zero on such an element, so the non-zero
+// entries of node i's row lie on the three coordinate lines through i.
+// rows[(a*npe + i)*(o+1) + m], axis a (0: x, 1: z, 2: y), element node i (local numbering
+// l + n(o+1) + m(o+1)^2): the entry toward the node of local index m along a.  The diagonal is
+// held whole by the x entry (m = i's own x index); the z and y entries there are zero.
+void reference_element_rows(const Gll &g, double jx, double jz, double jy, std::vector<float> &rows);
+
+// Node-class coefficients of the operator the reference assembles from those rows on a uniform
+// box: for an interior node with local indices (lx, lz, ly) in 0..o-1 (0: on element faces), the
+// coefficient of the node d places along axis a, summed exactly over the elements that hold both
+// nodes and rounded once to float; the diagonal sits in the x entry d = 0.
+// tab[(((a*o + ly)*o + lz)*(2o+1) + d + o)*o + lx].
+void reference_class_table(const Gll &g, double jx, double jz, double jy, std::vector<float> &tab);
+constexpr int reference_class_table_size(int o) { return 3 * o * o * (2 * o + 1) * o; }
+
 // Ricker wavelet in the reference's float arithmetic (utils.hpp:11-46).
 float ricker(float t, float f0, int order);
 

@@ -34,15 +34,15 @@ int coef_table_size(int order) { return 3 * (order + 1) * (order + 1); }
 
 namespace {
 
-template <int O>
+template <int O, bool REF = false>
 struct ElemCfg {
     static constexpr int O1 = O + 1, NP = O1 * O1, NPE = O1 * O1 * O1;
     static constexpr int TE = O <= 4 ? 32 : 16;  // elements per CTA
     static constexpr int CS = NPE | 1;  // odd row stride: lanes hit distinct banks
     static constexpr int THREADS = TE * NP;
     static constexpr int MINB = O == 1 ? 8 : O == 2 ? 5 : O == 3 ? 3 : O == 4 ? 2 : 2;
-    static constexpr size_t SMEM = sizeof(int) * 2 * TE * CS + sizeof(float) * NPE * TE * 3 +
-                                   sizeof(float) * 3 * NP;
+    static constexpr int TAB = REF ? 3 * NPE * O1 : 3 * NP;  // coefficient floats in shared memory
+    static constexpr size_t SMEM = sizeof(int) * 2 * TE * CS + sizeof(float) * NPE * TE * 3 + sizeof(float) * TAB;
 };
 
 // One direction of the element operator along one pencil: out = base * S p in difference form,
@@ -66,11 +66,11 @@ __device__ __forceinline__ void pencil_apply(const ElementArgs &a, const float (
     for (int i = 0; i <= O; i++) out[i] = base * acc[i];
 }
 
-template <int O>
+template <int O, bool REF>
 __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     k_element(const ElementArgs a)
 {
-    using C = ElemCfg<O>;
+    using C = ElemCfg<O, REF>;
     constexpr int O1 = C::O1, NP = C::NP, NPE = C::NPE, CS = C::CS, TE = C::TE;
     extern __shared__ __align__(16) unsigned char smem[];
     int *s_conn = reinterpret_cast<int *>(smem);  // [2][TE * CS]: this tile's rows and the next tile's
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     };
 
     // A: coefficient table, the first tile's rows, and its pencil values
-    for (int q = tid; q < 3 * NP; q += C::THREADS) s_tab[q] = __ldg(a.tab + q);
+    for (int q = tid; q < C::TAB; q += C::THREADS) s_tab[q] = __ldg((REF ? a.rtab : a.tab) + q);
     load_conn(t, 0);
     __syncthreads();
     float pn[O1];
@@ -125,32 +125,61 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
             s_p[(i + O1 * jx + NP * kx) * TE + lane] = px[i];
         }
         if (tn < ntiles) load_conn(tn, b ^ 1);
-        // C: x-direction in registers
         float yx[O1];
-        pencil_apply<O>(a, px, s_tab[0 * NP + jx + O1 * kx], yx);
-        __syncthreads();
-        if (tn < ntiles) gather(tn, b ^ 1, pn);
-        // D: z-direction (local index j varies) into s_y, and E: y-direction (local index k
-        // varies) into s_w; both only read s_p, so no barrier between them
-        {
-            const int i = warp % O1, k = warp / O1;
-            float pz[O1], yz[O1];
+        if constexpr (REF) {
+            __syncthreads();
+            if (tn < ntiles) gather(tn, b ^ 1, pn);
+            // C': K_e p at the thread's nodes as the reference forms it (SEMQkGLIntegrals.hpp:
+            // 508-513): Y = sum over the row in increasing local index j of R[j] p[j], multiply and
+            // add rounded separately.  The row's non-zero entries lie on the node's three lines;
+            // in increasing j: the y-line below the node, the z-line below it, the x-line, the
+            // z-line above, the y-line above.
 #pragma unroll
-            for (int m = 0; m < O1; m++) pz[m] = s_p[(i + O1 * m + NP * k) * TE + lane];
-            pencil_apply<O>(a, pz, s_tab[1 * NP + i + O1 * k], yz);
+            for (int i1 = 0; i1 < O1; i1++) {
+                const int node = i1 + O1 * jx + NP * kx;
+                const float *rx = s_tab + (0 * NPE + node) * O1;
+                const float *rz = s_tab + (1 * NPE + node) * O1;
+                const float *ry = s_tab + (2 * NPE + node) * O1;
+                float acc = 0.f;
+                for (int m = 0; m < kx; m++)
+                    acc = __fadd_rn(acc, __fmul_rn(ry[m], s_p[(i1 + O1 * jx + NP * m) * TE + lane]));
+                for (int m = 0; m < jx; m++)
+                    acc = __fadd_rn(acc, __fmul_rn(rz[m], s_p[(i1 + O1 * m + NP * kx) * TE + lane]));
 #pragma unroll
-            for (int m = 0; m < O1; m++) s_y[(i + O1 * m + NP * k) * TE + lane] = yz[m];
+                for (int m = 0; m < O1; m++) acc = __fadd_rn(acc, __fmul_rn(rx[m], px[m]));
+                for (int m = jx + 1; m < O1; m++)
+                    acc = __fadd_rn(acc, __fmul_rn(rz[m], s_p[(i1 + O1 * m + NP * kx) * TE + lane]));
+                for (int m = kx + 1; m < O1; m++)
+                    acc = __fadd_rn(acc, __fmul_rn(ry[m], s_p[(i1 + O1 * jx + NP * m) * TE + lane]));
+                yx[i1] = acc;
+            }
+        } else {
+            // C: x-direction in registers
+            pencil_apply<O>(a, px, s_tab[0 * NP + jx + O1 * kx], yx);
+            __syncthreads();
+            if (tn < ntiles) gather(tn, b ^ 1, pn);
+            // D: z-direction (local index j varies) into s_y, and E: y-direction (local index k
+            // varies) into s_w; both only read s_p, so no barrier between them
+            {
+                const int i = warp % O1, k = warp / O1;
+                float pz[O1], yz[O1];
+#pragma unroll
+                for (int m = 0; m < O1; m++) pz[m] = s_p[(i + O1 * m + NP * k) * TE + lane];
+                pencil_apply<O>(a, pz, s_tab[1 * NP + i + O1 * k], yz);
+#pragma unroll
+                for (int m = 0; m < O1; m++) s_y[(i + O1 * m + NP * k) * TE + lane] = yz[m];
+            }
+            {
+                const int i = warp % O1, j = warp / O1;
+                float py[O1], yy[O1];
+#pragma unroll
+                for (int n = 0; n < O1; n++) py[n] = s_p[(i + O1 * j + NP * n) * TE + lane];
+                pencil_apply<O>(a, py, s_tab[2 * NP + i + O1 * j], yy);
+#pragma unroll
+                for (int n = 0; n < O1; n++) s_w[(i + O1 * j + NP * n) * TE + lane] = yy[n];
+            }
+            __syncthreads();
         }
-        {
-            const int i = warp % O1, j = warp / O1;
-            float py[O1], yy[O1];
-#pragma unroll
-            for (int n = 0; n < O1; n++) py[n] = s_p[(i + O1 * j + NP * n) * TE + lane];
-            pencil_apply<O>(a, py, s_tab[2 * NP + i + O1 * j], yy);
-#pragma unroll
-            for (int n = 0; n < O1; n++) s_w[(i + O1 * j + NP * n) * TE + lane] = yy[n];
-        }
-        __syncthreads();
         // F: scatter through the connectivity.  The tile's elements are consecutive (one per
         // lane); where the next lane's element shares this element's right x-face (same global
         // nodes), its left-face value is added here with a shuffle and it skips that atomic.
@@ -160,7 +189,8 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
 #pragma unroll
             for (int i = 0; i < O1; i++) {
                 const int node = i + O1 * jx + NP * kx;
-                v[i] = act ? yx[i] + s_y[node * TE + lane] + s_w[node * TE + lane] : 0.f;
+                if constexpr (REF) v[i] = act ? yx[i] : 0.f;
+                else v[i] = act ? yx[i] + s_y[node * TE + lane] + s_w[node * TE + lane] : 0.f;
             }
             const int g_left = act ? cr[0 + O1 * jx + NP * kx] : -1;
             const int g_right = act ? cr[O + O1 * jx + NP * kx] : -2;
@@ -182,31 +212,40 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     }
 }
 
-template <int O>
-cudaError_t launch_element_t(const ElementArgs &a, cudaStream_t s)
+template <int O, bool REF>
+cudaError_t launch_element_r(const ElementArgs &a, cudaStream_t s)
 {
-    using C = ElemCfg<O>;
+    using C = ElemCfg<O, REF>;
     if (a.n_elem <= 0) return cudaSuccess;
     const int64_t tiles = (a.n_elem + C::TE - 1) / C::TE;
     // persistent CTAs: as many as are resident at once
     int dev = 0, sms = 152, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_element<O>, C::THREADS, C::SMEM) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_element<O, REF>, C::THREADS, C::SMEM) != cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
     const int64_t grid = std::min<int64_t>(tiles, (int64_t)sms * per_sm);
-    k_element<O><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(a);
+    k_element<O, REF><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(a);
     return cudaGetLastError();
+}
+
+template <int O>
+cudaError_t launch_element_t(const ElementArgs &a, cudaStream_t s)
+{
+    return a.rtab ? launch_element_r<O, true>(a, s) : launch_element_r<O, false>(a, s);
 }
 
 template <int O>
 cudaError_t setup_t()
 {
-    return cudaFuncSetAttribute(k_element<O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)ElemCfg<O>::SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_element<O, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)ElemCfg<O, false>::SMEM);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_element<O, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)ElemCfg<O, true>::SMEM);
 }
 
 }  // namespace

@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "stencil.h"
@@ -248,6 +249,54 @@ __device__ __forceinline__ VecG<O, NG> axis_uniform(const float (&c)[NG][O], con
     return r;
 }
 
+// Axis term of the reference-rounding pass: continues the node's accumulation r (x-term already
+// in it) with sum_{d!=0} C[d][j] row_g(d)[j], C the node-class coefficients of this axis
+// (cb + LOC*stride points to the [2o+1][o] block of the thread's class), in order of d.
+template <int O, int NG, int GS, int LOC, class RowFn>
+__device__ __forceinline__ VecG<O, NG> axis_class(VecG<O, NG> r, const float *cb0, int stride, const RowFn &row)
+{
+    const float *cb = cb0 + LOC * stride;
+#pragma unroll
+    for (int d = dlo(O, LOC); d <= dhi(O, LOC); d++) {
+        if (d == 0) continue;
+        const float *p = row(d);
+        const float *cd = cb + (d + O) * O;
+#pragma unroll
+        for (int g = 0; g < NG; g++) {
+            float v[O];
+            load_o<O>(p + g * GS, v);
+            if constexpr (SEM_STENCIL_PACKED_AXIS && O % 2 == 0) {
+#pragma unroll
+                for (int jp = 0; jp < O / 2; jp++) {
+                    const float2 acc = fma2(*reinterpret_cast<const float2 *>(cd + 2 * jp),
+                                            make_float2(v[2 * jp], v[2 * jp + 1]),
+                                            make_float2(r.v[g][2 * jp], r.v[g][2 * jp + 1]));
+                    r.v[g][2 * jp] = acc.x;
+                    r.v[g][2 * jp + 1] = acc.y;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < O; j++) r.v[g][j] = fmaf(cd[j], v[j], r.v[g][j]);
+            }
+        }
+    }
+    return r;
+}
+
+template <int O, int NG, int GS, class RowFn>
+__device__ __forceinline__ VecG<O, NG> axis_class_dispatch(int loc, const VecG<O, NG> &r, const float *cb0, int stride,
+                                                          const RowFn &row)
+{
+    switch (loc) {
+    case 0: return axis_class<O, NG, GS, 0>(r, cb0, stride, row);
+    case 1: if constexpr (O > 1) return axis_class<O, NG, GS, 1>(r, cb0, stride, row);
+    case 2: if constexpr (O > 2) return axis_class<O, NG, GS, 2>(r, cb0, stride, row);
+    case 3: if constexpr (O > 3) return axis_class<O, NG, GS, 3>(r, cb0, stride, row);
+    default: if constexpr (O > 4) return axis_class<O, NG, GS, 4>(r, cb0, stride, row);
+    }
+    return axis_class<O, NG, GS, 0>(r, cb0, stride, row);  // not reached: loc < O
+}
+
 template <int O, int NG, int GS, bool DIRECT, class RowFn>
 __device__ __forceinline__ VecG<O, NG> axis_dispatch(int loc, const float (&c)[NG][O], const RowFn &row)
 {
@@ -282,12 +331,21 @@ struct YPlanes {
     }
 };
 
-template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI>
+struct NoClassTable {
+    int unused;
+};
+template <int O, bool REF>
+using ClassParam = typename std::conditional<REF, ClassTable<O>, NoClassTable>::type;
+
+// REF: the reference-rounding operator -- every coefficient from the node-class table `ct`, one
+// accumulation per node over the x-, z- and y-terms (direct form only).
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF = false>
 __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap win_map,
               const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap a_map,
-              const StencilTables t, const StencilArgs a)
+              const StencilTables t, const StencilArgs a, const __grid_constant__ ClassParam<O, REF> ct)
 {
+    static_assert(!REF || DIRECT, "the reference-rounding operator is a direct form");
     using C = Cfg<O>;
     constexpr int TZ = C::TZ, TX = C::TX, HX = C::HX, TXP = C::TXP, R = C::R, AUX = C::AUX;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -444,11 +502,15 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
 
             // x: local index j is compile-time
             float ax[NG][O];
+            // REF: the class coefficients of the thread's nodes along x, [2o+1][o]
+            const float *cx = nullptr;
+            if constexpr (REF) cx = &ct.c[0][ly][lz][0][0];
 #pragma unroll
             for (int g = 0; g < NG; g++)
 #pragma unroll
                 for (int j = 0; j < O; j++) {
-                    float acc = DIRECT ? c_T[O - 1][j * (2 * O + 1) + O] * c[g][j] : 0.f;
+                    float acc = REF ? cx[O * O + j] * c[g][j]
+                                    : (DIRECT ? c_T[O - 1][j * (2 * O + 1) + O] * c[g][j] : 0.f);
                     // constant trip count, so that the loop unrolls together with j and every
                     // index below is a constant (a j-dependent range left it rolled, with the
                     // arrays in memory)
@@ -457,14 +519,28 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
                         if (d == 0 || d < dlo(O, j) || d > dhi(O, j)) continue;
                         const int m = j + d;  // offset from the thread's first node, in [-O, O]
                         const float v = m < 0 ? left[g][m + O] : (m < O ? c[g][m] : right[g]);
-                        acc = fmaf(c_T[O - 1][j * (2 * O + 1) + d + O], DIRECT ? v : v - c[g][j], acc);
+                        acc = fmaf(REF ? cx[(d + O) * O + j] : c_T[O - 1][j * (2 * O + 1) + d + O],
+                                   DIRECT ? v : v - c[g][j], acc);
                     }
                     ax[g][j] = acc;
                 }
-            const VecG<O, NG> az = axis_dispatch<O, NG, GR * TXP, DIRECT>(lz, c, ZRows{cur, TXP});
             const float *yb0 = ring + rs * C::RING_FLOATS + toff;
             const YPlanes<R, C::RING_FLOATS> yrows{yb0, yb0 + R * C::RING_FLOATS, yb0 - R * C::RING_FLOATS, rs};
-            const VecG<O, NG> ay = axis_dispatch<O, NG, GR * TX, DIRECT>(ly, c, yrows);
+            VecG<O, NG> az, ay;
+            if constexpr (REF) {
+                // one accumulation per node: x-terms, then z-terms, then y-terms, in order of d
+                VecG<O, NG> r;
+#pragma unroll
+                for (int g = 0; g < NG; g++)
+#pragma unroll
+                    for (int j = 0; j < O; j++) r.v[g][j] = ax[g][j];
+                constexpr int WO = (2 * O + 1) * O;
+                r = axis_class_dispatch<O, NG, GR * TXP>(lz, r, &ct.c[1][ly][0][0][0], WO, ZRows{cur, TXP});
+                ay = axis_class_dispatch<O, NG, GR * TX>(ly, r, &ct.c[2][0][lz][0][0], O * WO, yrows);
+            } else {
+                az = axis_dispatch<O, NG, GR * TXP, DIRECT>(lz, c, ZRows{cur, TXP});
+                ay = axis_dispatch<O, NG, GR * TX, DIRECT>(ly, c, yrows);
+            }
 
             const bool yin = y > 0 && y < ny - 1;
             const float wy = c_wa[O - 1][ly];
@@ -484,11 +560,14 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
                                                  : make_float2(1.f, 1.f);
                         const float2 q2 = make_float2(q[g][j], q[g][j + 1]);
                         const float2 qd2 = SPONGE ? mul2(s2, q2) : q2;
-                        const float2 y2 =
-                            fma2(make_float2(c_wa[O - 1][j], c_wa[O - 1][j + 1]),
-                                 fma2(make_float2(gyz, gyz), make_float2(ay.v[g][j], ay.v[g][j + 1]),
-                                      mul2(make_float2(gzy, gzy), make_float2(az.v[g][j], az.v[g][j + 1]))),
-                                 mul2(make_float2(gx, gx), make_float2(ax[g][j], ax[g][j + 1])));
+                        float2 y2;
+                        if constexpr (REF)
+                            y2 = make_float2(ay.v[g][j], ay.v[g][j + 1]);
+                        else
+                            y2 = fma2(make_float2(c_wa[O - 1][j], c_wa[O - 1][j + 1]),
+                                      fma2(make_float2(gyz, gyz), make_float2(ay.v[g][j], ay.v[g][j + 1]),
+                                           mul2(make_float2(gzy, gzy), make_float2(az.v[g][j], az.v[g][j + 1]))),
+                                      mul2(make_float2(gx, gx), make_float2(ax[g][j], ax[g][j + 1])));
                         // (2c - qd) - am*y: 2c is exact, then one fused multiply-add
                         const float2 t2 = sub2(mul2(make_float2(2.f, 2.f), make_float2(c[g][j], c[g][j + 1])), qd2);
                         const float2 o2 = fma2(make_float2(-am[g][j], -am[g][j + 1]), y2, t2);
@@ -501,7 +580,11 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
                         constexpr int j = O - 1;
                         sv[g][j] = SPONGE ? sxz[g][j] * syv : 1.f;
                         qdv[g][j] = SPONGE ? sv[g][j] * q[g][j] : q[g][j];
-                        const float yv = fmaf(c_wa[O - 1][j], fmaf(gyz, ay.v[g][j], gzy * az.v[g][j]), gx * ax[g][j]);
+                        float yv;
+                        if constexpr (REF)
+                            yv = ay.v[g][j];
+                        else
+                            yv = fmaf(c_wa[O - 1][j], fmaf(gyz, ay.v[g][j], gzy * az.v[g][j]), gx * ax[g][j]);
                         out[g][j] = (2.f * c[g][j] - qdv[g][j]) - am[g][j] * yv;
                         if (MODE == STENCIL_RECORD_KP) kp[g][j] = yv;
                     }
@@ -515,7 +598,11 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
                         sv[g][j] = SPONGE ? sxz[g][j] * syv : 1.f;
                         qdv[g][j] = SPONGE ? sv[g][j] * q[g][j] : q[g][j];
                         // K.p at the node: g1 Wz Wy A_x + Wx (g2 Wy A_z + g3 Wz A_y)
-                        const float yv = fmaf(wxj, fmaf(gyz, ay.v[g][j], gzy * az.v[g][j]), gx * ax[g][j]);
+                        float yv;
+                        if constexpr (REF)
+                            yv = ay.v[g][j];
+                        else
+                            yv = fmaf(wxj, fmaf(gyz, ay.v[g][j], gzy * az.v[g][j]), gx * ax[g][j]);
                         out[g][j] = (2.f * c[g][j] - qdv[g][j]) - am[g][j] * yv;
                         if (MODE == STENCIL_RECORD_KP) kp[g][j] = yv;
                     }
@@ -653,18 +740,37 @@ int blocks_per_sm(int order)
     }
 }
 
-template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI>
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF = false>
 void launch_om(const dim3 &grid, const LevelMaps &cm, const LevelMaps &pm, const StencilTables &t,
                const StencilArgs &a, cudaStream_t s)
 {
-    k_stencil<O, SPONGE, MODE, DIRECT, MULTI>
-        <<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.tile, cm.win, pm.tile, t.amap, t, a);
+    ClassParam<O, REF> ct{};
+    if constexpr (REF) std::memcpy(ct.c, t.class_tab, sizeof ct.c);
+    k_stencil<O, SPONGE, MODE, DIRECT, MULTI, REF>
+        <<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.tile, cm.win, pm.tile, t.amap, t, a, ct);
 }
 
 template <int O, bool DIRECT>
 cudaError_t launch_of(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, int mode, cudaStream_t s)
 {
     const LevelMaps &cm = t.lv[ci], &pm = t.lv[1 - ci];
+    if (t.class_tab) {
+        // reference rounding: plain steps with the node-class table (one shot or many)
+        if constexpr (DIRECT) {
+            if (mode != STENCIL_PLAIN) return cudaErrorInvalidValue;
+            if (t.nshot > 1) {
+                const dim3 grid((unsigned)((int64_t)t.grid[0] * t.grid[1] * t.nshot), (unsigned)t.grid[2]);
+                if (sponge) launch_om<O, true, STENCIL_PLAIN, true, true, true>(grid, cm, pm, t, a, s);
+                else launch_om<O, false, STENCIL_PLAIN, true, true, true>(grid, cm, pm, t, a, s);
+            } else {
+                const dim3 grid(t.grid[0], t.grid[1], t.grid[2]);
+                if (sponge) launch_om<O, true, STENCIL_PLAIN, true, false, true>(grid, cm, pm, t, a, s);
+                else launch_om<O, false, STENCIL_PLAIN, true, false, true>(grid, cm, pm, t, a, s);
+            }
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
+    }
     if (t.nshot > 1) {
         // many shots: plain steps in the direct form
         if constexpr (DIRECT) {
@@ -696,10 +802,10 @@ cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, int ci, bool 
     return direct ? launch_of<O, true>(t, a, ci, sponge, mode, s) : launch_of<O, false>(t, a, ci, sponge, mode, s);
 }
 
-template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI = false>
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI = false, bool REF = false>
 cudaError_t setup_om()
 {
-    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE, DIRECT, MULTI>,
+    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE, DIRECT, MULTI, REF>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<O>::SMEM);
 }
 
@@ -722,6 +828,10 @@ cudaError_t setup_o()
     if (e == cudaSuccess) e = setup_of<O, false>();
     if (e == cudaSuccess) e = setup_om<O, true, STENCIL_PLAIN, true, true>();
     if (e == cudaSuccess) e = setup_om<O, false, STENCIL_PLAIN, true, true>();
+    if (e == cudaSuccess) e = setup_om<O, true, STENCIL_PLAIN, true, false, true>();
+    if (e == cudaSuccess) e = setup_om<O, false, STENCIL_PLAIN, true, false, true>();
+    if (e == cudaSuccess) e = setup_om<O, true, STENCIL_PLAIN, true, true, true>();
+    if (e == cudaSuccess) e = setup_om<O, false, STENCIL_PLAIN, true, true, true>();
     return e;
 }
 
@@ -840,9 +950,21 @@ cudaError_t stencil_set_receivers(StencilTables &t, const int64_t *sorted_nodes,
     return cudaMemcpy(t.d_rec_idx, idx.data(), nrec * sizeof(int), cudaMemcpyHostToDevice);
 }
 
+int stencil_set_class_table(StencilTables &t, const float *tab)
+{
+    delete[] t.class_tab;
+    t.class_tab = nullptr;
+    if (!tab) return 0;
+    const size_t n = (size_t)reference_class_table_size(t.order);
+    t.class_tab = new float[n];
+    std::memcpy(t.class_tab, tab, n * sizeof(float));
+    return 0;
+}
+
 void stencil_tables_free(StencilTables *&t)
 {
     if (!t) return;
+    delete[] t->class_tab;
     if (t->d_rec_off) cudaFree(t->d_rec_off);
     if (t->d_rec_idx) cudaFree(t->d_rec_idx);
     delete t;

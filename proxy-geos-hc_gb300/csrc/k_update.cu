@@ -38,7 +38,9 @@ __global__ void k_source(const SourceArgs a)
     }
 }
 
-template <bool SPONGE>
+// REF: the reference's update arithmetic, (2 p^n - p^{n-1}) - ((dt*dt) y) / M, each operation
+// rounded (SEMsolver.cpp:85-89), with M in a.mref; otherwise the precomputed a = dt^2/M.
+template <bool SPONGE, bool REF>
 __global__ void __launch_bounds__(kUpdateThreads) k_update(const UpdateArgs a)
 {
     constexpr int V = kUpdateNodesPerThread;
@@ -50,7 +52,7 @@ __global__ void __launch_bounds__(kUpdateThreads) k_update(const UpdateArgs a)
         const float4 c4 = *reinterpret_cast<const float4 *>(a.cur + i0);
         const float4 q4 = *reinterpret_cast<const float4 *>(a.prev + i0);
         const float4 y4 = *reinterpret_cast<const float4 *>(a.y + i0);
-        const float4 a4 = __ldg(reinterpret_cast<const float4 *>(a.a + i0));
+        const float4 a4 = __ldg(reinterpret_cast<const float4 *>((REF ? a.mref : a.a) + i0));
         const float cc[V] = {c4.x, c4.y, c4.z, c4.w}, qq[V] = {q4.x, q4.y, q4.z, q4.w};
         const float yy[V] = {y4.x, y4.y, y4.z, y4.w}, aa[V] = {a4.x, a4.y, a4.z, a4.w};
         const bool zy_in = iz > 0 && iz < a.nz - 1 && iy > 0 && iy < a.ny - 1;
@@ -66,7 +68,13 @@ __global__ void __launch_bounds__(kUpdateThreads) k_update(const UpdateArgs a)
                 if (SPONGE) s = __ldg(a.sx + ix) * syz * szv;  // (sx*sy)*sz
                 const float qd = SPONGE ? s * qq[t] : qq[t];
                 const bool interior = zy_in && ix > 0 && ix < a.nx - 1;
-                const float v = interior ? (2.f * cc[t] - qd) - aa[t] * yy[t] : qd;
+                float v = qd;
+                if (interior) {
+                    if constexpr (REF)
+                        v = __fsub_rn(__fsub_rn(2.f * cc[t], qd), __fdiv_rn(__fmul_rn(a.dt2f, yy[t]), aa[t]));
+                    else
+                        v = (2.f * cc[t] - qd) - aa[t] * yy[t];
+                }
                 out[t] = SPONGE ? s * v : v;
             }
         }
@@ -159,6 +167,39 @@ __global__ void k_mass(float *a, const double *inv_c2, const float *slow2, int e
         }
 }
 
+// The reference's assembled mass (SEMsolver.cpp:74-78, SEMQkGLIntegrals.hpp:352): for each
+// adjacent element in increasing element order, M += fl(fl(w_a w_b w_c detJ) / fl(c_e c_e)), the
+// local weights by the node's local indices in that element, all in float.  Padding nodes get 1.
+__global__ void k_mass_ref(float *m, const float *vel, int ex, int ey, int ez, int order, int nxp, const double *w,
+                           double detJ)
+{
+    const int nx = ex * order + 1, ny = ey * order + 1, nz = ez * order + 1;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ix >= nxp) return;
+    int x0 = 0, x1 = 0;
+    if (ix < nx) adj_range(ix, order, ex, x0, x1);
+    for (int iy = blockIdx.z; iy < ny; iy += gridDim.z)
+        for (int iz = blockIdx.y; iz < nz; iz += gridDim.y) {
+            const int64_t q = ix + (int64_t)nxp * (iz + (int64_t)nz * iy);
+            if (ix >= nx) {
+                m[q] = 1.f;
+                continue;
+            }
+            int z0, z1, y0, y1;
+            adj_range(iz, order, ez, z0, z1);
+            adj_range(iy, order, ey, y0, y1);
+            float sum = 0.f;
+            for (int ey_ = y0; ey_ <= y1; ey_++)
+                for (int ez_ = z0; ez_ <= z1; ez_++)
+                    for (int ex_ = x0; ex_ <= x1; ex_++) {
+                        const float ml = (float)(w[ix - ex_ * order] * w[iz - ez_ * order] * w[iy - ey_ * order] * detJ);
+                        const float c = vel[ex_ + (int64_t)ex * (ez_ + (int64_t)ez * ey_)];
+                        sum = __fadd_rn(sum, __fdiv_rn(ml, __fmul_rn(c, c)));
+                    }
+            m[q] = sum;
+        }
+}
+
 // g_i <- g_i / m_i with m_i the node's squared slowness, recovered from the stored
 // a_i = dt^2 / (m_i W_i) and the geometric mass W_i (quadrature weight x detJ x adjacent elements),
 // so it holds for element-velocity and node-slowness models alike.
@@ -198,8 +239,23 @@ cudaError_t launch_update(const UpdateArgs &a, bool sponge, cudaStream_t s)
     if (a.n_int <= 0) return cudaSuccess;
     const int64_t grid = update_grid(a.n_int);
     if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
-    if (sponge) k_update<true><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
-    else k_update<false><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
+    if (a.mref) {
+        if (sponge) k_update<true, true><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
+        else k_update<false, true><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
+    } else {
+        if (sponge) k_update<true, false><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
+        else k_update<false, false><<<(unsigned)grid, kUpdateThreads, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mass_ref(float *m, const float *vel, int ex, int ey, int ez, int order, int64_t nxp,
+                            const double *w_dev, double detJ, cudaStream_t s)
+{
+    const int64_t ny = (int64_t)ey * order + 1, nz = (int64_t)ez * order + 1;
+    const dim3 grid((unsigned)((nxp + 127) / 128), (unsigned)std::min<int64_t>(nz, 65535),
+                    (unsigned)std::min<int64_t>(ny, 65535));
+    k_mass_ref<<<grid, 128, 0, s>>>(m, vel, ex, ey, ez, order, (int)nxp, w_dev, detJ);
     return cudaGetLastError();
 }
 

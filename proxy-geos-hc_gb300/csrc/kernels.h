@@ -34,6 +34,9 @@ struct ElementArgs {
     const float *tab;    // coef table (device)
     int64_t n_elem;
     float S[6][6];       // 1-D element stiffness S[i][m] = sum_l w_l phi_i'(xi_l) phi_m'(xi_l)
+    // SEM_ROUNDING_REFERENCE: the reference's element rows (device, float, layout of
+    // reference_element_rows); null: the 1-D stiffness above in difference form
+    const float *rtab;
 };
 
 struct UpdateArgs {
@@ -50,6 +53,10 @@ struct UpdateArgs {
     int nrec;
     float *traces;       // [step][nrec]
     const int *ctr;      // ctr[1] = index of the step being run
+    // SEM_ROUNDING_REFERENCE: the reference's float mass M (launch_mass_ref) and fl(dt*dt); the
+    // update then rounds as the reference does.  Null: the precomputed a = dt^2/M.
+    const float *mref;
+    float dt2f;
 };
 
 struct SourceArgs {
@@ -67,7 +74,7 @@ constexpr int kUpdateNodesPerThread = 4;
 constexpr int64_t kUpdateNodesPerBlock = (int64_t)kUpdateThreads * kUpdateNodesPerThread;
 inline int64_t update_grid(int64_t n) { return (n + kUpdateNodesPerBlock - 1) / kUpdateNodesPerBlock; }
 
-cudaError_t launch_element(int order, const ElementArgs &a, cudaStream_t s);
+cudaError_t launch_element(int order, const ElementArgs &a, cudaStream_t s);  // a.rtab selects the rows
 cudaError_t launch_update(const UpdateArgs &a, bool sponge, cudaStream_t s);
 cudaError_t launch_source(const SourceArgs &a, cudaStream_t s);
 cudaError_t launch_connectivity(int32_t *conn, int ex, int ey, int ez, int order, int64_t nxp,
@@ -80,6 +87,9 @@ cudaError_t launch_grad_scale(float *g, const float *a, int ex, int ey, int ez, 
 cudaError_t launch_mass(float *a, const float *vel, const float *slow2, int ex, int ey, int ez,
                         int order, int64_t nxp, const double *w_dev, double detJ, double dt2,
                         cudaStream_t s);
+// The reference's float mass M_i per node from per-element velocity (device layout; padding 1).
+cudaError_t launch_mass_ref(float *m, const float *vel, int ex, int ey, int ez, int order, int64_t nxp,
+                            const double *w_dev, double detJ, cudaStream_t s);
 cudaError_t element_kernel_setup();
 
 }  // namespace semgb

@@ -16,6 +16,7 @@ struct sem_solver {
     bool own_stream = false;
     int kernel = SEM_KERNEL_AUTO;
     int form = SEM_FORM_DIRECT;  // operator form of the stencil pass
+    int rounding = SEM_ROUNDING_DEFAULT;  // SEM_ROUNDING_REFERENCE: the reference's rounded rows
     int64_t n_int = 0;               // nodes of the device layout
     float *d_p[2] = {nullptr, nullptr};
     int cur = 0;                 // index of the current level
@@ -23,6 +24,9 @@ struct sem_solver {
     float *d_a = nullptr;        // dt^2 / M
     uint64_t a_version = 0;
     float *d_tab = nullptr;      // element coefficient table
+    float *d_rtab = nullptr;     // SEM_ROUNDING_REFERENCE: the reference's element rows (element path)
+    float *d_mref = nullptr;     // SEM_ROUNDING_REFERENCE: the reference's float mass (element path)
+    uint64_t mref_version = 0;
     double *d_w = nullptr;       // GLL weights (double) for the mass kernel
     semgb::StencilTables *stencil = nullptr;
     // sponge

@@ -25,8 +25,18 @@ struct LevelMaps {
     CUtensorMap tile;   // tile width x TZ rows x 1 plane
 };
 
+// Node-class coefficients of the reference-rounding pass (layout of reference_class_table:
+// [axis][ly][lz][d + o][lx]), handed to the kernel by value as a __grid_constant__ parameter.
+template <int O>
+struct alignas(16) ClassTable {
+    float c[3][O][O][2 * O + 1][O];
+};
+
 struct StencilTables {
     int order = 0;
+    // SEM_ROUNDING_REFERENCE: the reference's assembled node-class coefficients, host memory
+    // owned by the tables (null: the tensor-product operator below)
+    float *class_tab = nullptr;
     int64_t nx = 0, nxp = 0, ny = 0, nz = 0;
     float g[3] = {0, 0, 0};   // g_d = |detJ| / J_dd^2 for x (xi1), z (xi2), y (xi3)
     float wa[6] = {0};        // assembled weight by local index: wa[0] = 2 w_0, wa[l] = w_l
@@ -75,6 +85,9 @@ int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int n
 int stencil_bind(StencilTables &t, const float *p0, const float *p1, const float *a);
 // Group node-sorted receivers (device-layout indices) by owning CTA (device CSR in t).
 cudaError_t stencil_set_receivers(StencilTables &t, const int64_t *sorted_nodes, int nrec, uint64_t version);
+// Switch the pass to the reference-rounding operator with node-class table `tab` (layout of
+// reference_class_table, copied), or back to the tensor-product operator (tab null).
+int stencil_set_class_table(StencilTables &t, const float *tab);
 void stencil_tables_free(StencilTables *&t);
 cudaError_t stencil_kernel_setup();
 // cur_index: which of the bound pressure buffers is the current level.

@@ -21,6 +21,7 @@ LIB_PATH = os.environ.get("SEMGB_LIBRARY") or os.path.join(_HERE, "_lib", "libse
 SEM_OK, SEM_ERR_ARG, SEM_ERR_CUDA, SEM_ERR_OOM, SEM_ERR_TIMEOUT, SEM_ERR_UNSTABLE, SEM_ERR_STATE = range(7)
 KERNEL_AUTO, KERNEL_ELEMENT, KERNEL_STENCIL = 0, 1, 2
 FORM_DIRECT, FORM_DIFFERENCE = 0, 1
+ROUNDING_DEFAULT, ROUNDING_REFERENCE = 0, 1
 LEVEL_CURRENT, LEVEL_PREVIOUS = 0, 1
 
 _I64P = C.POINTER(C.c_int64)
@@ -48,6 +49,8 @@ _SIGS = {
     "sem_box_element_from_point": [C.c_int] * 3 + [C.c_float] * 6 + [_I64P],
     "sem_box_nearest_node": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int] + [C.c_float] * 3 + [_I64P],
     "sem_box_sponge_profile": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int, C.c_int, C.c_float, _F32P, _F32P, _F32P],
+    "sem_box_refround_rows": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int, _F32P],
+    "sem_box_refround_class_table": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int, _F32P],
     "sem_mesh_create_box": [C.c_int] * 3 + [C.c_float] * 3 + [C.c_int, C.POINTER(_VP)],
     "sem_mesh_destroy": [_VP],
     "sem_mesh_info": [_VP, _I64P, _I64P, C.POINTER(C.c_int), _I64P],
@@ -59,6 +62,7 @@ _SIGS = {
     "sem_solver_set_stream": [_VP, _VP],
     "sem_solver_set_kernel": [_VP, C.c_int],
     "sem_solver_set_operator_form": [_VP, C.c_int],
+    "sem_solver_set_rounding": [_VP, C.c_int],
     "sem_solver_set_sponge": [_VP, C.c_int, C.c_float],
     "sem_solver_set_sponge_profile": [_VP, _F32P, _F32P, _F32P],
     "sem_solver_set_sources": [_VP, C.c_int, _I64P, _F32P, C.c_int],
@@ -221,6 +225,22 @@ def sponge_profile(ex, ey, ez, lx, ly, lz, order, thickness, sigma):
     return tuple(f)
 
 
+def refround_rows(ex, ey, ez, lx, ly, lz, order):
+    """The reference's float-rounded element rows, [3][(o+1)^3][o+1] (see semgb.h)."""
+    o1 = order + 1
+    out = np.empty(3 * o1 ** 4, np.float32)
+    _check(lib().sem_box_refround_rows(ex, ey, ez, lx, ly, lz, order, _p(out, _F32P)))
+    return out.reshape(3, o1 ** 3, o1)
+
+
+def refround_class_table(ex, ey, ez, lx, ly, lz, order):
+    """Node-class coefficients of the reference's assembled operator, [3][ly][lz][2o+1][lx]."""
+    o = order
+    out = np.empty(3 * o * o * (2 * o + 1) * o, np.float32)
+    _check(lib().sem_box_refround_class_table(ex, ey, ez, lx, ly, lz, order, _p(out, _F32P)))
+    return out.reshape(3, o, o, 2 * o + 1, o)
+
+
 # ---- device objects ---------------------------------------------------------------------------
 
 class Mesh:
@@ -295,6 +315,10 @@ class Solver:
     def set_operator_form(self, form: int):
         """FORM_DIRECT (default, fastest) or FORM_DIFFERENCE (exact on constant fields)."""
         _check(lib().sem_solver_set_operator_form(self._h, form))
+
+    def set_rounding(self, rounding: int):
+        """ROUNDING_DEFAULT or ROUNDING_REFERENCE (the reference's float-rounded element rows)."""
+        _check(lib().sem_solver_set_rounding(self._h, rounding))
 
     def set_sponge(self, thickness: int, sigma: float):
         _check(lib().sem_solver_set_sponge(self._h, thickness, sigma))
