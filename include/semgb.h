@@ -13,8 +13,8 @@
  *    caller unless a name says "device".  Functions that return data synchronise the solver's
  *    stream first; sem_solver_step only enqueues work.  Whole fields (pressure levels, squared
  *    slowness, gradients) cross through the library's pinned staging buffers, so the caller's
- *    arrays may be ordinary pageable memory; the first such copy in a process pins 32 MB of host
- *    memory, kept until the process exits.
+ *    arrays may be ordinary pageable memory; the first such copy on each device pins 32 MB of
+ *    host memory for that device, kept until the process exits.
  *  - A handle is used by one host thread at a time; separate solvers may run on separate streams.
  *  - Node numbering is the reference's: node = ix + iz*nx + iy*nx*nz with nx = ex*order+1 etc.
  *    (SEMmesh.cpp:142-231); element e = ix + iz*ex + iy*ex*ez; coordinates are (x, y, z).
@@ -359,16 +359,22 @@ int sem_adjoint_get_adjoint_traces(sem_adjoint *a, float *out);
  * coefficient table live in a fixed array of 4,194,304 floats (16 MiB) in the library's device
  * image, so the mesh may have at most 4,194,176 nodes; larger meshes are rejected with
  * SEM_ERR_ARG.  All buffers are device memory in the reference node numbering:
- *   conn    int32 [n_elem][(order+1)^3] element-to-node map (as sem_mesh_get_connectivity gives)
+ *   conn    int32 [n_elem][(order+1)^3] element-to-node map (as sem_mesh_get_connectivity gives);
+ *           entries must lie in [0, n_nodes): one outside is skipped (read as 0, not scattered)
  *   p_cur   current level; sponge-damped in place when sponge factors are given
  *   p_prev  previous level (already damped); replaced by the new level
  *   coef    dt^2 / M_i per node
  *   sx, sy, sz  per-axis sponge factors (sem_box_sponge_profile), or all three NULL
  * Sources are the caller's: add them to p_cur before the call.  Work is enqueued on `stream`
  * (a cudaStream_t; NULL is the legacy default stream).  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) and caches it; make that first call before
- * any stream capture.  Every call uses the same array, which keeps the last call's contents
- * (the call clears what it needs): calls whose work overlaps on the GPU race on it. */
+ * the array's device address (cudaGetSymbolAddress) and caches it, and loads the device code
+ * of the kernels the step launches; under CUDA's lazy module loading that is when the driver
+ * places the library's code and the 16 MiB array in device memory.  So make that first call
+ * before the caller's pool manager reserves device memory, and before any stream capture; later
+ * calls leave the device's free memory unchanged.  The cached address does not survive
+ * cudaDeviceReset (nor does any other handle of this library).  Every call uses the same array,
+ * which keeps the last call's contents (the call clears what it needs): calls whose work
+ * overlaps on the GPU race on it. */
 int sem_element_step_noalloc(int ex, int ey, int ez, float lx, float ly, float lz, int order,
                              const int32_t *conn, float *p_cur, float *p_prev, const float *coef,
                              const float *sx, const float *sy, const float *sz, void *stream);

@@ -10,11 +10,17 @@
 # two headers and a one-line commonConfig.hpp into oracle/_ref/shadow_q<order>/, which is put
 # first on the include path.  Everything written goes under oracle/_ref/ (git-ignored).
 #
-# Usage: oracle/build_ref.sh [reference-root]      (default: /root/reference)
+# Usage: oracle/build_ref.sh [reference-root]
+# The root of the reference checkout comes from the argument or else from SEMGB_REFERENCE_ROOT;
+# with neither, nothing is built (the tests that need the compiled reference then skip).
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${SEMGB_REFERENCE_ROOT:-}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
+if [ -z "$REF" ]; then
+    echo "no reference checkout given (argument or SEMGB_REFERENCE_ROOT): compiled reference not built" >&2
+    exit 0
+fi
 if [ ! -f "$REF/src/sem/solver/SEMsolver.cpp" ]; then
     echo "reference sources not found under $REF" >&2
     exit 1

@@ -37,35 +37,57 @@ void solver_invalidate_graphs(sem_solver *s)
 
 namespace {
 
-// Process-wide pinned staging for field_to_host / field_from_host (allocated on first use, kept
-// for the life of the process; calls from several threads take turns).
+// Pinned staging for field_to_host / field_from_host, one set per device (its events must live
+// on the device of the stream they are recorded on); allocated on first use on that device and
+// kept for the life of the process; calls from several threads take turns.
 struct Staging {
     static constexpr int64_t kFloats = int64_t(4) << 20;  // 16 MB per buffer
     std::mutex mu;
+    int device = -1;
     float *buf[2] = {nullptr, nullptr};
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaError_t init()
     {
-        cudaError_t e = cudaSuccess;
+        if (device < 0) return cudaErrorInvalidDevice;
+        int prev = 0;
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e == cudaSuccess && prev != device) e = cudaSetDevice(device);
         for (int k = 0; k < 2 && e == cudaSuccess; k++) {
             if (!buf[k]) e = cudaHostAlloc(reinterpret_cast<void **>(&buf[k]), kFloats * 4, cudaHostAllocDefault);
             if (e == cudaSuccess && !ev[k]) e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
         }
+        if (prev != device) cudaSetDevice(prev);
         return e;
     }
 };
 
-Staging &staging()
+constexpr int kMaxStagingDevices = 64;
+
+// The staging of the device that stream s belongs to (null if that device cannot be told).
+Staging *staging(cudaStream_t s)
 {
-    static Staging st;
-    return st;
+    static Staging st[kMaxStagingDevices];
+    int dev = -1;
+    if (cudaStreamGetDevice(s, &dev) != cudaSuccess) {
+        cudaGetLastError();
+        if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    }
+    if (dev < 0 || dev >= kMaxStagingDevices) return nullptr;
+    st[dev].device = dev;
+    return &st[dev];
 }
 
 }  // namespace
 
 cudaError_t field_to_host(float *dst, const float *src, int64_t nx, int64_t nxp, int64_t rows, cudaStream_t s)
 {
-    Staging &st = staging();
+    Staging *stp = staging(s);
+    if (!stp) {
+        cudaGetLastError();
+        cudaError_t e = cudaMemcpy2DAsync(dst, nx * 4, src, nxp * 4, nx * 4, rows, cudaMemcpyDeviceToHost, s);
+        return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+    }
+    Staging &st = *stp;
     std::lock_guard<std::mutex> lock(st.mu);
     if (nx > Staging::kFloats || st.init() != cudaSuccess) {
         cudaGetLastError();
@@ -97,7 +119,13 @@ cudaError_t field_to_host(float *dst, const float *src, int64_t nx, int64_t nxp,
 
 cudaError_t field_from_host(float *dst, const float *src, int64_t nx, int64_t nxp, int64_t rows, cudaStream_t s)
 {
-    Staging &st = staging();
+    Staging *stp = staging(s);
+    if (!stp) {
+        cudaGetLastError();
+        cudaError_t e = cudaMemcpy2DAsync(dst, nxp * 4, src, nx * 4, nx * 4, rows, cudaMemcpyHostToDevice, s);
+        return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+    }
+    Staging &st = *stp;
     std::lock_guard<std::mutex> lock(st.mu);
     if (nx > Staging::kFloats || st.init() != cudaSuccess) {
         cudaGetLastError();

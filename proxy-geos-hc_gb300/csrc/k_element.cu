@@ -66,7 +66,9 @@ __device__ __forceinline__ void pencil_apply(const ElementArgs &a, const float (
     for (int i = 0; i <= O; i++) out[i] = base * acc[i];
 }
 
-template <int O, bool REF>
+// REF: the reference's rows in its order (SEM_ROUNDING_REFERENCE).  CHECKED: caller-supplied
+// connectivity, every index checked against [0, a.n_check) before it is used.
+template <int O, bool REF, bool CHECKED = false>
 __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     k_element(const ElementArgs a)
 {
@@ -102,7 +104,10 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
         const bool act = lane < (int)min((int64_t)TE, a.n_elem - u * TE);
         const int *cr = s_conn + b * TE * CS + lane * CS;
 #pragma unroll
-        for (int i = 0; i < O1; i++) v[i] = act ? __ldg(a.p + cr[i + O1 * jx + NP * kx]) : 0.f;
+        for (int i = 0; i < O1; i++) {
+            const int g = cr[i + O1 * jx + NP * kx];
+            v[i] = act && (!CHECKED || (g >= 0 && g < a.n_check)) ? __ldg(a.p + g) : 0.f;
+        }
     };
 
     // A: coefficient table, the first tile's rows, and its pencil values
@@ -204,7 +209,9 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
 #pragma unroll
                 for (int i = 0; i < O1; i++) {
                     if (i == 0 && merged_into_prev) continue;
-                    atomicAdd(a.y + cr[i + O1 * jx + NP * kx], v[i]);  // result unused: compiles to RED
+                    const int g = cr[i + O1 * jx + NP * kx];
+                    if (CHECKED && !(g >= 0 && g < a.n_check)) continue;
+                    atomicAdd(a.y + g, v[i]);  // result unused: compiles to RED
                 }
             }
         }
@@ -212,7 +219,7 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     }
 }
 
-template <int O, bool REF>
+template <int O, bool REF, bool CHECKED = false>
 cudaError_t launch_element_r(const ElementArgs &a, cudaStream_t s)
 {
     using C = ElemCfg<O, REF>;
@@ -222,30 +229,38 @@ cudaError_t launch_element_r(const ElementArgs &a, cudaStream_t s)
     int dev = 0, sms = 152, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_element<O, REF>, C::THREADS, C::SMEM) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_element<O, REF, CHECKED>, C::THREADS, C::SMEM) !=
+            cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
     const int64_t grid = std::min<int64_t>(tiles, (int64_t)sms * per_sm);
-    k_element<O, REF><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(a);
+    k_element<O, REF, CHECKED><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
 template <int O>
 cudaError_t launch_element_t(const ElementArgs &a, cudaStream_t s)
 {
+    if (a.n_check > 0) return a.rtab ? cudaErrorInvalidValue : launch_element_r<O, false, true>(a, s);
     return a.rtab ? launch_element_r<O, true>(a, s) : launch_element_r<O, false>(a, s);
+}
+
+template <int O, bool REF, bool CHECKED>
+cudaError_t setup_one()
+{
+    return cudaFuncSetAttribute(k_element<O, REF, CHECKED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)ElemCfg<O, REF>::SMEM);
 }
 
 template <int O>
 cudaError_t setup_t()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_element<O, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)ElemCfg<O, false>::SMEM);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_element<O, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)ElemCfg<O, true>::SMEM);
+    cudaError_t e = setup_one<O, false, false>();
+    if (e == cudaSuccess) e = setup_one<O, true, false>();
+    if (e == cudaSuccess) e = setup_one<O, false, true>();
+    return e;
 }
 
 }  // namespace

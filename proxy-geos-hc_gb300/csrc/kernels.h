@@ -37,6 +37,10 @@ struct ElementArgs {
     // SEM_ROUNDING_REFERENCE: the reference's element rows (device, float, layout of
     // reference_element_rows); null: the 1-D stiffness above in difference form
     const float *rtab;
+    // > 0: connectivity entries come from the caller and are checked against [0, n_check):
+    // an entry outside is never read or written through (its gather reads 0, its scatter is
+    // dropped).  0: the library built the map, no checks.
+    int64_t n_check;
 };
 
 struct UpdateArgs {

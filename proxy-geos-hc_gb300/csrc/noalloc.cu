@@ -87,7 +87,9 @@ __global__ void k_update_ref(float *p_cur, float *p_prev, float *y, const float 
 }
 
 // Device address of the scratch array on the current device: resolved on the first call made
-// with that device current, then cached.
+// with that device current, then cached.  That first call also loads, under CUDA's lazy module
+// loading, the code of every kernel the step launches and the array itself: this is the one
+// point at which the entry point can make the driver allocate device memory.
 int scratch_for_current_device(float **out)
 {
     int dev = 0;
@@ -109,6 +111,9 @@ int scratch_for_current_device(float **out)
             return SEM_ERR_CUDA;
         }
         e = element_kernel_setup();
+        cudaFuncAttributes fa;
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_fill_tab);
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_update_ref);
         if (e != cudaSuccess) {
             set_last_error(std::string("element kernel set-up: ") + cudaGetErrorString(e));
             return SEM_ERR_CUDA;
@@ -165,6 +170,7 @@ extern "C" int sem_element_step_noalloc(int ex, int ey, int ez, float lx, float 
     ea.y = y;
     ea.tab = tab;
     ea.n_elem = b.n_elem;
+    ea.n_check = b.n_nodes;  // the caller's map: indices outside [0, n_nodes) are skipped
     element_stiffness_1d(g, ea.S);
 
     // the array keeps the last call's contents: clear the accumulator this call uses

@@ -4,9 +4,12 @@ whose time loop runs where allocation is not allowed).
 
 The test calls the entry point through the C ABI on device buffers the test owns, twice in a row,
 and compares each result with the solver's element step (sem_solver_step with
-SEM_KERNEL_ELEMENT) from the same state.  Both paths use the same element kernel with float
-atomics, so sums may round differently in the last bit; the tolerance is relative L2 <= 2e-6.
-This file is collected last so that a failure here leaves every other test already run.
+SEM_KERNEL_ELEMENT) from the same state and with the oracle (the reference's arithmetic on the
+CPU).  Both GPU paths use the same element kernel with float atomics, so sums may round
+differently in the last bit; the tolerance is relative L2 <= 2e-6 against the solver and 5e-6
+against the oracle.  After the first call (which loads the library's device code), a call must
+leave the device's free memory unchanged.  This file is collected last so that a failure here
+leaves every other test already run.
 """
 import ctypes as C
 
@@ -71,6 +74,12 @@ def test_noalloc_step_matches_solver_element_step(semgb_lib, cuda_device):
         s.step(1)
         expect.append((s.pressure(semgb.LEVEL_CURRENT), s.pressure(semgb.LEVEL_PREVIOUS)))
 
+    # the oracle: the reference's arithmetic for the same two steps
+    from oracle import oracle as O
+    P = O.Problem(wl.ex, wl.ey, wl.ez, o, wl.lx, wl.ly, wl.lz, wl.dt, 2, np.ascontiguousarray(wl.vel, np.float32),
+                  np.zeros(0, np.int64), np.zeros((0, 2), np.float32), sponge32=sp)
+    oracle_out = [O.run(P.__class__(**{**P.__dict__, "nsteps": n}), p0, q0) for n in (1, 2)]
+
     # the allocation-free entry point on buffers this test owns
     dev = torch.device("cuda", 0)
     conn = torch.from_numpy(mesh.connectivity()).to(dev)
@@ -78,9 +87,11 @@ def test_noalloc_step_matches_solver_element_step(semgb_lib, cuda_device):
     sxyz = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in sp]
     levels = [torch.from_numpy(p0).to(dev), torch.from_numpy(q0).to(dev)]
     stream = torch.cuda.current_stream(dev)
+    torch.cuda.synchronize(dev)
     cur = 0
     for k in range(2):
         pc, pp = levels[cur], levels[1 - cur]
+        free_before = torch.cuda.mem_get_info(dev)[0]
         rc = lib.sem_element_step_noalloc(wl.ex, wl.ey, wl.ez, wl.lx, wl.ly, wl.lz, o,
                                           C.c_void_p(conn.data_ptr()), C.c_void_p(pc.data_ptr()),
                                           C.c_void_p(pp.data_ptr()), C.c_void_p(coef.data_ptr()),
@@ -88,6 +99,9 @@ def test_noalloc_step_matches_solver_element_step(semgb_lib, cuda_device):
                                           C.c_void_p(stream.cuda_stream))
         assert rc == semgb.SEM_OK, lib.sem_last_error_string().decode()
         torch.cuda.synchronize(dev)
+        free_after = torch.cuda.mem_get_info(dev)[0]
+        if k > 0:  # the first call in a process may load device code; later calls allocate nothing
+            assert free_after == free_before, (free_before, free_after)
         new, damped_old = pp.cpu().numpy(), pc.cpu().numpy()
         cur = 1 - cur
         e_new = rel_l2(new, expect[k][0])
@@ -95,6 +109,9 @@ def test_noalloc_step_matches_solver_element_step(semgb_lib, cuda_device):
         assert e_new <= 2e-6, (k, e_new)
         assert e_old <= 2e-6, (k, e_old)
         assert np.isfinite(new).all()
+        o_new, o_old, _ = oracle_out[k]
+        assert rel_l2(new, o_new) <= 5e-6, (k, rel_l2(new, o_new))
+        assert rel_l2(damped_old, o_old) <= 5e-6, (k, rel_l2(damped_old, o_old))
 
 
 def test_noalloc_rejects_meshes_beyond_its_scratch(semgb_lib, cuda_device):
@@ -108,3 +125,43 @@ def test_noalloc_rejects_meshes_beyond_its_scratch(semgb_lib, cuda_device):
                                       None, None, None, None)
     assert rc == semgb.SEM_ERR_ARG
     assert b"at most" in lib.sem_last_error_string()
+
+
+def test_noalloc_skips_connectivity_outside_the_mesh(semgb_lib, cuda_device):
+    """Entries of the caller's map outside [0, n_nodes) are never read or written through: a map
+    with one element's row pointing past the mesh changes nothing outside the mesh's nodes (the
+    buffers are padded with sentinels that must survive)."""
+    import torch
+
+    from semgb import workloads as W
+
+    semgb = semgb_lib
+    lib = semgb.lib()
+    wl = W.small_random(4, 3, 3, 2, 1, seed=32, nsrc=0, nrec=0, sponge=0)
+    o = wl.order
+    mesh = semgb.Mesh(wl.ex, wl.ey, wl.ez, wl.lx, wl.ly, wl.lz, o)
+    N = mesh.n_nodes
+    conn = mesh.connectivity().copy()
+    conn[5, :] = N + 7        # past the mesh: inside the padded buffers below
+    conn[6, 3] = -1           # negative
+    dev = torch.device("cuda", 0)
+    pad = 64
+    sentinel = 12345.0
+    levels = []
+    rng = np.random.default_rng(3)
+    for _ in range(2):
+        a = np.full(N + pad, sentinel, np.float32)
+        a[:N] = rng.standard_normal(N).astype(np.float32)
+        levels.append(torch.from_numpy(a).to(dev))
+    coef = torch.full((N + pad,), 1e-3, device=dev)
+    c = torch.from_numpy(conn).to(dev)
+    rc = lib.sem_element_step_noalloc(wl.ex, wl.ey, wl.ez, wl.lx, wl.ly, wl.lz, o, C.c_void_p(c.data_ptr()),
+                                      C.c_void_p(levels[0].data_ptr()), C.c_void_p(levels[1].data_ptr()),
+                                      C.c_void_p(coef.data_ptr()), None, None, None,
+                                      C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    assert rc == semgb.SEM_OK, lib.sem_last_error_string().decode()
+    torch.cuda.synchronize(dev)
+    for lv in levels:
+        tail = lv.cpu().numpy()[N:]
+        assert np.all(tail == sentinel)
+        assert np.isfinite(lv.cpu().numpy()[:N]).all()
