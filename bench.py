@@ -177,7 +177,7 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     wl = make_workload(args.workload, args.elems)
-    n = args.ref_elems
+    n = args.cpu_elems
     sw = cpu_sample(wl, n)
     from oracle import oracle as O
     O.lib()
@@ -342,6 +342,7 @@ def run_ours(args):
             mesh.close()
             torch.cuda.synchronize()
             line["rows"] = {"operator_forms": measure_forms(args.elems), "orders": measure_orders(), "element_path": measure_element(args.elems, args.steps),
+                            "rounding": measure_rounding(args.elems),
                             "batched": measure_batched(), "uneven": measure_uneven(),
                             "uneven_small": measure_uneven(200, 8, 24, "c3_uneven_32_small"), "adjoint": measure_adjoint(),
                             "learned_boundary": measure_learned()}
@@ -382,6 +383,31 @@ def measure_forms(n: int = 200, steps: int = 20):
         s.step(4)
         ms = _ev_time(stream, lambda: s.step(steps)) / steps
         out[name] = {"ms_per_step": ms, "Gnode_steps_per_s": mesh.n_nodes / (ms / 1e3) / 1e9}
+        s.close()
+        mesh.close()
+    return out
+
+
+def measure_rounding(n: int = 200, steps: int = 20):
+    """The stencil pass on the headline workload in both roundings of the operator: the build's
+    own (default) and the reference's float-rounded element rows (sem_solver_set_rounding), which
+    keeps FP32 results within 1e-5 of the reference on long runs; node-steps/s and the fraction
+    of the measured HBM bandwidth at 16 B per node."""
+    import torch
+    import semgb
+    wl = make_workload("c2", n)
+    peak, _ = hbm_peak()
+    out = {}
+    for name, rnd in (("default", semgb.ROUNDING_DEFAULT), ("reference", semgb.ROUNDING_REFERENCE)):
+        mesh, s = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
+        s.set_rounding(rnd)
+        stream = torch.cuda.Stream()
+        s.set_stream(stream.cuda_stream)
+        s.step(4)
+        ms = _ev_time(stream, lambda: s.step(steps)) / steps
+        N = mesh.n_nodes
+        out[name] = {"ms_per_step": ms, "Gnode_steps_per_s": N / (ms / 1e3) / 1e9,
+                     "frac": 16.0 * N / (ms / 1e3) / 1e9 / peak}
         s.close()
         mesh.close()
     return out
@@ -704,9 +730,10 @@ def main():
     ap.add_argument("--workload", choices=["c2", "c1"], default="c2")
     ap.add_argument("--kernel", choices=["auto", "element", "stencil"], default="auto")
     ap.add_argument("--elems", type=int, default=200, help="elements per axis of the c2 recipe")
-    ap.add_argument("--cpu-elems", type=int, default=40, help="cpu_baseline sub-box (elements per axis)")
-    ap.add_argument("--cpu-steps", type=int, default=16, help="cpu_baseline steps")
-    ap.add_argument("--ref-elems", type=int, default=32, help="--impl reference sub-box (elements per axis)")
+    ap.add_argument("--cpu-elems", type=int, default=100,
+                    help="CPU sub-box of the workload (elements per axis), timed by both the cpu_baseline leg "
+                         "and --impl reference")
+    ap.add_argument("--cpu-steps", type=int, default=6, help="cpu_baseline steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-rows", action="store_true", help="skip the element-path / batched / uneven / adjoint / learned-boundary rows")
     ap.add_argument("--case", choices=["batch40", "abc86", "q5_80"], default=None,

@@ -287,10 +287,12 @@ int sem_batch_get_traces(sem_batch *b, float *out);
 int sem_batch_get_pressure(sem_batch *b, int shot, int level, float *out);
 /* Time n_steps (CUDA events on the batch's stream); advances the batch. */
 int sem_batch_time_step(sem_batch *b, int n_steps, float *ms_per_step);
-/* Time the candidate launch shapes (planes per CTA along y; one shot per CTA and 8 warps per CTA
- * are fixed) on the current state, keep the fastest, restore the state; any output pointer may
- * be NULL. */
-int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, int *ychunk);
+/* Time the candidate launch shapes on the current state, keep the fastest, restore the state:
+ * shots per thread-block cluster (the CTAs of that many consecutive shots of a tile start
+ * together and share the mass tiles through L2; 1, 2, 4 or 8, dividing the shot count) by planes
+ * per CTA along y.  warps_per_cta reports the pass's fixed CTA width.  Any output pointer may be
+ * NULL. */
+int sem_batch_autotune(sem_batch *b, int *shots_per_cluster, int *warps_per_cta, int *ychunk);
 
 /* ------------------------------------------------------------------------------------------
  * Groups of independent problems of uneven size (different meshes, orders, models, dt).  The

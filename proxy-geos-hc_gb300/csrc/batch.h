@@ -8,12 +8,13 @@
 
 namespace semgb {
 
-// Launch shape the autotuner picks (sem_batch_autotune).  The stencil pass fixes the first two;
-// the y-chunk length is the one knob.
+// Launch shape the autotuner picks (sem_batch_autotune): the CTAs of how many consecutive shots
+// of a tile run as one thread-block cluster, and the y-chunk length; the stencil pass fixes the
+// warps per CTA.
 struct BatchTuning {
-    int shots_per_lane = 1;  // one shot per CTA: the CTAs of all shots of a tile run together
-    int warps_per_cta = 8;
-    int ychunk = 0;          // planes per CTA along y (0: the stencil pass's own choice)
+    int shots_per_cluster = 1;  // 1, 2, 4 or 8 (a divisor of the shot count)
+    int warps_per_cta = 4;
+    int ychunk = 0;             // planes per CTA along y (0: the stencil pass's own choice)
 };
 
 struct BatchSourceArgs {

@@ -196,8 +196,7 @@ int sem_batch_create(sem_mesh *m, float dt, int n_shots, sem_batch **out)
         return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     if ((e = stencil_kernel_setup()) != cudaSuccess) return cleanup(SEM_ERR_CUDA, std::string("kernel set-up: ") + cudaGetErrorString(e));
     if (stencil_tables_create(m->box, m->gll, m->geo, n_shots, &b->st) != 0) return cleanup(SEM_ERR_CUDA, "stencil tables");
-    b->tune.shots_per_lane = 1;
-    b->tune.warps_per_cta = 8;
+    b->tune.warps_per_cta = b->st->threads / 32;
     b->tune.ychunk = b->st->ychunk;
     *out = b;
     return SEM_OK;
@@ -446,7 +445,7 @@ int sem_batch_time_step(sem_batch *b, int n_steps, float *ms_per_step)
     GUARD_END
 }
 
-int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, int *ychunk)
+int sem_batch_autotune(sem_batch *b, int *shots_per_cluster, int *warps_per_cta, int *ychunk)
 {
     GUARD_BEGIN
     if (!b) return sem_fail(SEM_ERR_ARG, "NULL batch");
@@ -463,19 +462,26 @@ int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, in
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
-    int pick = b->st->ychunk;
-    for (int chunk : candidates(b, b->st->ychunk)) {
-        cudaError_t err = set_chunk(b, chunk);
-        const StencilArgs a = args_for(b, b->cur, false);
-        if (err == cudaSuccess) err = launch_stencil(*b->st, a, b->cur, b->sponge, b->stream);  // warm-up
-        cudaEventRecord(e0, b->stream);
-        for (int r = 0; r < 3 && err == cudaSuccess; r++) err = launch_stencil(*b->st, a, b->cur, b->sponge, b->stream);
-        cudaEventRecord(e1, b->stream);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (err == cudaSuccess && ms < best) { best = ms; pick = b->st->ychunk; }
+    int pick = b->st->ychunk, pick_cluster = b->st->cluster;
+    const std::vector<int> chunks = candidates(b, b->st->ychunk);
+    for (int cl : {1, 2, 4, 8}) {
+        if (b->nshot % cl != 0) continue;
+        b->st->cluster = cl;
+        for (int chunk : chunks) {
+            cudaError_t err = set_chunk(b, chunk);
+            const StencilArgs a = args_for(b, b->cur, false);
+            if (err == cudaSuccess) err = launch_stencil(*b->st, a, b->cur, b->sponge, b->stream);  // warm-up
+            cudaEventRecord(e0, b->stream);
+            for (int r = 0; r < 3 && err == cudaSuccess; r++) err = launch_stencil(*b->st, a, b->cur, b->sponge, b->stream);
+            cudaEventRecord(e1, b->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (err != cudaSuccess) cudaGetLastError();  // a shape the device cannot launch: skipped
+            else if (ms < best) { best = ms; pick = b->st->ychunk; pick_cluster = cl; }
+        }
     }
+    b->st->cluster = pick_cluster;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     CUDA_TRY(cudaMemcpyAsync(b->d_p[1 - b->cur], keep, n * 4, cudaMemcpyDeviceToDevice, b->stream));
@@ -483,9 +489,10 @@ int sem_batch_autotune(sem_batch *b, int *shots_per_lane, int *warps_per_cta, in
     dfree(keep);
     CUDA_TRY(set_chunk(b, pick));
     b->tune.ychunk = pick;
+    b->tune.shots_per_cluster = pick_cluster;
     b->tuned = true;
     invalidate(b);
-    if (shots_per_lane) *shots_per_lane = b->tune.shots_per_lane;
+    if (shots_per_cluster) *shots_per_cluster = b->tune.shots_per_cluster;
     if (warps_per_cta) *warps_per_cta = b->tune.warps_per_cta;
     if (ychunk) *ychunk = pick;
     return SEM_OK;

@@ -746,6 +746,26 @@ void launch_om(const dim3 &grid, const LevelMaps &cm, const LevelMaps &pm, const
 {
     ClassParam<O, REF> ct{};
     if constexpr (REF) std::memcpy(ct.c, t.class_tab, sizeof ct.c);
+    if (MULTI && t.cluster > 1) {
+        // the CTAs of `cluster` consecutive shots of a tile (consecutive in x of the grid) start
+        // together on one GPC and march along y side by side, so each dt^2/M tile they share is
+        // still in L2 when the later ones read it
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = grid;
+        cfg.blockDim = dim3(Cfg<O>::THREADS);
+        cfg.dynamicSmemBytes = Cfg<O>::SMEM;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)t.cluster;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_stencil<O, SPONGE, MODE, DIRECT, MULTI, REF>, cm.tile, cm.win, pm.tile, t.amap, t,
+                           a, ct);
+        return;
+    }
     k_stencil<O, SPONGE, MODE, DIRECT, MULTI, REF>
         <<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.tile, cm.win, pm.tile, t.amap, t, a, ct);
 }
@@ -881,6 +901,7 @@ int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int n
     for (int l = 0; l < b.order; l++) t->wa[l] = (float)(l == 0 ? g.w[0] + g.w[b.order] : g.w[l]);
     int threads = 256;
     tile_dims(b.order, t->tile_x, t->tile_z, t->halo_x, threads);
+    t->threads = threads;
     t->smem = smem_bytes(b.order);
     t->grid[0] = (int)((b.nx + t->tile_x - 1) / t->tile_x);
     t->grid[1] = (int)((b.nz + t->tile_z - 1) / t->tile_z);

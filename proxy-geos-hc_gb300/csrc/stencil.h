@@ -41,8 +41,11 @@ struct StencilTables {
     float g[3] = {0, 0, 0};   // g_d = |detJ| / J_dd^2 for x (xi1), z (xi2), y (xi3)
     float wa[6] = {0};        // assembled weight by local index: wa[0] = 2 w_0, wa[l] = w_l
     int tile_x = 0, tile_z = 0, halo_x = 0;
+    int threads = 0;          // per CTA
     int grid[3] = {0, 0, 0};  // tiles along x, z and y-chunks (launch: x * z * nshot CTAs by chunks)
     int nshot = 1;            // shots stacked along y in the levels (many-shot form)
+    int cluster = 1;          // many-shot form: CTAs of consecutive shots of a tile co-scheduled as
+                              // one thread-block cluster (divides nshot; 1: plain launch)
     int64_t shot_stride = 0;  // floats per shot field: nxp * nz * ny
     int ychunk = 0;           // planes per CTA
     size_t smem = 0;          // dynamic shared memory per CTA

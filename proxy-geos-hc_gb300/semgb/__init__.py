@@ -516,7 +516,7 @@ class Batch:
     def autotune(self):
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         _check(lib().sem_batch_autotune(self._h, C.byref(a), C.byref(b), C.byref(c)))
-        return {"shots_per_lane": a.value, "warps_per_cta": b.value, "ychunk": c.value}
+        return {"shots_per_cluster": a.value, "warps_per_cta": b.value, "ychunk": c.value}
 
 
 class Group:

@@ -63,7 +63,7 @@ def test_batch_autotune_keeps_state(semgb_lib, cuda_device):
         b.step(20)
         if tune:
             pick = b.autotune()
-            assert pick["shots_per_lane"] == 1 and pick["warps_per_cta"] == 8
+            assert pick["shots_per_cluster"] in (1, 2, 4, 8) and pick["warps_per_cta"] >= 1
         b.step(40)
         res.append((b.traces(), b.pressure(7)))
         b.close()
