@@ -43,6 +43,17 @@ struct sem_abc {
     int64_t n_shell = 0;
     float *d_hist = nullptr;     // [n_int]
     float *d_corr = nullptr;     // [n]
+    // layer 0: face tiles (abc_face) and a second history buffer: a step reads p^{n-1} from
+    // hbuf[hcur] and writes p^n into the other
+    bool face = false;
+    int4 *d_tiles = nullptr;
+    int64_t ntiles = 0;
+    int64_t *d_pos = nullptr;
+    float *d_hist_alt = nullptr;
+    int hcur = 0;
+    FaceDesc faces[6];
+    float *hist_now() const { return face && hcur ? d_hist_alt : d_hist; }
+    float *hist_next() const { return face && !hcur ? d_hist_alt : d_hist; }
 };
 
 namespace {
@@ -63,7 +74,7 @@ AbcArgs abc_args(const sem_abc *a)
     x.n = a->n;
     x.p_new = s->d_p[s->cur];      // after a step the new level is the current one
     x.p_cur = s->d_p[1 - s->cur];  // and p^n the stored previous one
-    x.hist = a->d_hist;
+    x.hist = a->hist_now();
     x.sx = s->sponge ? s->d_sx : nullptr;
     x.sy = s->sponge ? s->d_sy : nullptr;
     x.sz = s->sponge ? s->d_sz : nullptr;
@@ -81,6 +92,25 @@ cudaError_t enqueue_correction(sem_abc *a)
 {
     sem_solver *s = a->s;
     const AbcArgs x = abc_args(a);
+    if (a->face) {
+        AbcFaceArgs f{};
+        for (int k = 0; k < 6; k++) f.face[k] = a->faces[k];
+        f.tiles = a->d_tiles;
+        f.ntiles = a->ntiles;
+        f.pos = a->d_pos;
+        f.p_new = x.p_new;
+        f.p_cur = x.p_cur;
+        f.hist = a->hist_now();
+        f.hist_next = a->hist_next();
+        f.sx = x.sx; f.sy = x.sy; f.sz = x.sz;
+        f.nx = x.nx; f.nxp = x.nxp; f.ny = x.ny; f.nz = x.nz;
+        f.corr = a->d_corr;
+        cudaError_t e = abc_face(a->net->dev(), f, s->stream);
+        if (e != cudaSuccess) return e;
+        if ((e = abc_apply(x, s->d_p[s->cur], nullptr, s->stream)) != cudaSuccess) return e;
+        a->hcur ^= 1;
+        return cudaSuccess;
+    }
     cudaError_t e = abc_correction(a->net->dev(), x, s->stream);
     if (e != cudaSuccess) return e;
     if ((e = abc_apply(x, s->d_p[s->cur], a->d_hist, s->stream)) != cudaSuccess) return e;
@@ -271,6 +301,9 @@ int sem_abc_destroy(sem_abc *a)
     dfree(a->d_shell);
     dfree(a->d_hist);
     dfree(a->d_corr);
+    dfree(a->d_tiles);
+    dfree(a->d_pos);
+    dfree(a->d_hist_alt);
     delete a;
     return SEM_OK;
 }
@@ -308,6 +341,45 @@ int sem_abc_create(sem_solver *s, sem_mlp *net, int layer_elems, sem_abc **out)
     if (e == cudaSuccess) e = cudaMemcpy(a->d_nodes, nodes.data(), nodes.size() * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(a->d_shell, shell.data(), shell.size() * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(a->d_hist, 0, (size_t)b.n_int * 4);
+    if (e == cudaSuccess && layer_elems == 0) {
+        // face tiles: y-faces whole, z-faces without the rows on y-faces, x-faces without the
+        // rows on y- and z-faces, so every boundary node lies on one face
+        const int64_t nx = b.nx, ny = b.ny, nz = b.nz;
+        const int64_t dims[3] = {nx, ny, nz};
+        struct Spec { int n, u, v; int64_t ulo, uhi, vlo, vhi; };
+        const Spec spec[3] = {{1, 0, 2, 0, nx, 0, nz}, {2, 0, 1, 0, nx, 1, ny - 1}, {0, 2, 1, 1, nz - 1, 1, ny - 1}};
+        std::vector<int4> tiles;
+        std::vector<int64_t> pos;
+        for (int k = 0; k < 6; k++) {
+            const Spec &sp = spec[k / 2];
+            FaceDesc &f = a->faces[k];
+            f.axis_n = sp.n; f.axis_u = sp.u; f.axis_v = sp.v;
+            f.side = (k % 2 == 0) ? 0 : (int)(dims[sp.n] - 1);
+            f.inward = (k % 2 == 0) ? 1 : -1;
+            f.ulo = (int)sp.ulo; f.uhi = (int)sp.uhi; f.vlo = (int)sp.vlo; f.vhi = (int)sp.vhi;
+            for (int64_t v0 = sp.vlo; v0 < sp.vhi; v0 += kFaceTV)
+                for (int64_t u0 = sp.ulo; u0 < sp.uhi; u0 += kFaceTU) {
+                    tiles.push_back(make_int4(k, (int)u0, (int)v0, 0));
+                    for (int r = 0; r < kMlpTile; r++) {
+                        const int64_t u = u0 + r % kFaceTU, v = v0 + r / kFaceTU;
+                        if (u >= sp.uhi || v >= sp.vhi) { pos.push_back(-1); continue; }
+                        int64_t c[3];
+                        c[sp.u] = u; c[sp.v] = v; c[sp.n] = f.side;
+                        const int64_t qn = c[0] + c[2] * b.nxp + c[1] * b.nxp * b.nz;
+                        const auto it = std::lower_bound(nodes.begin(), nodes.end(), qn);
+                        pos.push_back(it != nodes.end() && *it == qn ? (int64_t)(it - nodes.begin()) : -1);
+                    }
+                }
+        }
+        a->face = true;
+        a->ntiles = (int64_t)tiles.size();
+        e = dalloc(&a->d_tiles, tiles.size());
+        if (e == cudaSuccess) e = dalloc(&a->d_pos, pos.size());
+        if (e == cudaSuccess) e = dalloc(&a->d_hist_alt, (size_t)b.n_int);
+        if (e == cudaSuccess) e = cudaMemcpy(a->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(a->d_pos, pos.data(), pos.size() * 8, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemset(a->d_hist_alt, 0, (size_t)b.n_int * 4);
+    }
     if (e != cudaSuccess) {
         sem_abc_destroy(a);
         return sem_fail(SEM_ERR_OOM, cudaGetErrorString(e));
@@ -342,6 +414,8 @@ int sem_abc_reset(sem_abc *a)
     if (!a) return sem_fail(SEM_ERR_ARG, "NULL boundary");
     CUDA_TRY(cudaStreamSynchronize(a->s->stream));
     CUDA_TRY(cudaMemset(a->d_hist, 0, (size_t)a->s->mesh->box.n_int * 4));
+    if (a->d_hist_alt) CUDA_TRY(cudaMemset(a->d_hist_alt, 0, (size_t)a->s->mesh->box.n_int * 4));
+    a->hcur = 0;
     return SEM_OK;
     GUARD_END
 }
@@ -352,7 +426,7 @@ int sem_abc_set_history(sem_abc *a, const float *p_prev)
     if (!a || !p_prev) return sem_fail(SEM_ERR_ARG, "NULL argument");
     const Box &b = a->s->mesh->box;
     CUDA_TRY(cudaStreamSynchronize(a->s->stream));
-    CUDA_TRY(field_from_host(a->d_hist, p_prev, b.nx, b.nxp, b.nz * b.ny, a->s->stream));
+    CUDA_TRY(field_from_host(a->hist_now(), p_prev, b.nx, b.nxp, b.nz * b.ny, a->s->stream));
     return SEM_OK;
     GUARD_END
 }
@@ -397,7 +471,7 @@ int sem_abc_features(sem_abc *a, float *x, float *scale)
     std::vector<float> pn(b.n_int), pc(b.n_int), ph(b.n_int);
     CUDA_TRY(cudaMemcpy(pn.data(), s->d_p[s->cur], b.n_int * 4, cudaMemcpyDeviceToHost));
     CUDA_TRY(cudaMemcpy(pc.data(), s->d_p[1 - s->cur], b.n_int * 4, cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(ph.data(), a->d_hist, b.n_int * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(ph.data(), a->hist_now(), b.n_int * 4, cudaMemcpyDeviceToHost));
     std::vector<float> sx(b.nx, 1.f), sy(b.ny, 1.f), sz(b.nz, 1.f);
     if (s->sponge) {
         CUDA_TRY(cudaMemcpy(sx.data(), s->d_sx, b.nx * 4, cudaMemcpyDeviceToHost));

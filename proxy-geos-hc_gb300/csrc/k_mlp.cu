@@ -643,6 +643,136 @@ __global__ void __launch_bounds__(128, 4) k_abc_correction(const MlpDev net, con
     }
 }
 
+constexpr int kPU = kFaceTU + 2, kPV = kFaceTV + 2, kPD = kPU * kPV;  // patch plane with its rim
+constexpr int kPL = 3 * kPD;  // one level: depth planes outside (zeros), face, inside
+// shared layout after the weights: xs, scale, then the patch [3 levels][3 depths][kPV][kPU] and
+// the 27 neighbour offsets
+constexpr size_t kFaceXsOff = kAbcXsOff;
+constexpr size_t kFacePatchOff = kFaceXsOff + sizeof(uint16_t) * T * KP1 + sizeof(float) * T;
+constexpr size_t kFaceOffsOff = kFacePatchOff + sizeof(float) * 3 * kPL;
+
+__global__ void __launch_bounds__(128, 4) k_abc_face(const MlpDev net, const AbcFaceArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
+    uint16_t *xs = reinterpret_cast<uint16_t *>(smem + kFaceXsOff);
+    float *scale = reinterpret_cast<float *>(xs + T * KP1);
+    float *patch = reinterpret_cast<float *>(smem + kFacePatchOff);
+    int *offs = reinterpret_cast<int *>(smem + kFaceOffsOff);
+    load_net(s, net);
+    // the depth plane outside the box stays zero for every tile
+    for (int i = threadIdx.x; i < 3 * kPD; i += blockDim.x) patch[(i / kPD) * kPL + i % kPD] = 0.f;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    const int64_t plane = a.nxp * a.nz;
+    for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        __syncthreads();  // the previous tile's patch, offsets and rows are consumed
+        const int4 td = a.tiles[t];
+        const FaceDesc f = a.face[td.x];
+        const int u0 = td.y, v0 = td.z;
+        if (threadIdx.x < 27) {
+            // feature neighbour nb = (dz+1)*9 + (dy+1)*3 + (dx+1) -> offset within a level's patch
+            const int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
+            auto along = [&](int axis) { return axis == 0 ? dx : (axis == 1 ? dy : dz); };
+            offs[threadIdx.x] = along(f.axis_n) * f.inward * kPD + along(f.axis_v) * kPU + along(f.axis_u);
+        }
+        // stage the face and inside planes of the three levels with a one-node rim; x-faces step
+        // through the depth fastest (adjacent in memory), the others along u (rows along x)
+        const bool depth_fast = f.axis_n == 0;
+        for (int i = threadIdx.x; i < 3 * 2 * kPD; i += blockDim.x) {
+            int l, di, vv, uu;
+            if (depth_fast) {
+                di = i % 2 + 1;
+                const int r = i / 2;
+                uu = r % kPU; vv = (r / kPU) % kPV; l = r / kPD;
+            } else {
+                uu = i % kPU;
+                const int r = i / kPU;
+                vv = r % kPV; di = (r / kPV) % 2 + 1; l = r / (2 * kPV);
+            }
+            const int cu = u0 - 1 + uu, cv = v0 - 1 + vv, cn = f.side + (di - 1) * f.inward;
+            // node coordinates by axis (selects, not an indexed array: it stays in registers)
+            const int cx = f.axis_u == 0 ? cu : (f.axis_v == 0 ? cv : cn);
+            const int cy = f.axis_u == 1 ? cu : (f.axis_v == 1 ? cv : cn);
+            const int cz = f.axis_u == 2 ? cu : (f.axis_v == 2 ? cv : cn);
+            float val = 0.f;
+            const bool in = cx >= 0 && cx < a.nx && cy >= 0 && cy < a.ny && cz >= 0 && cz < a.nz;
+            if (in) {
+                const int64_t c[3] = {cx, cy, cz};
+                const int64_t qn = c[0] + c[2] * a.nxp + c[1] * plane;
+                if (l == 0) {
+                    val = a.p_new[qn];
+                } else if (l == 1) {
+                    val = a.p_cur[qn];
+                    if (a.sx) val = val * ((__ldg(a.sx + c[0]) * __ldg(a.sy + c[1])) * __ldg(a.sz + c[2]));
+                    // p^n of the tile's own nodes and their inside neighbours: the next step's
+                    // p^{n-1} (every node of the two-node shell is one of these for some tile)
+                    const int us = u0 - 1 + uu, vs = v0 - 1 + vv;
+                    if (uu >= 1 && uu <= kFaceTU && vv >= 1 && vv <= kFaceTV && us < f.uhi && vs < f.vhi)
+                        a.hist_next[qn] = val;
+                } else {
+                    val = a.hist[qn];
+                }
+            }
+            patch[l * kPL + di * kPD + vv * kPU + uu] = val;
+        }
+        __syncthreads();
+        // features of the row's node from the patch (as k_abc_correction gathers them)
+        const int r = threadIdx.x;
+        const int64_t pos = a.pos[t * T + r];
+        const int base = kPD + (r / kFaceTU + 1) * kPU + (r % kFaceTU + 1);
+        uint16_t *xr = xs + r * KP1;
+        if (pos >= 0) {
+            float v[3][27];
+#pragma unroll
+            for (int l = 0; l < 3; l++)
+#pragma unroll
+                for (int nb = 0; nb < 27; nb++) v[l][nb] = patch[l * kPL + base + offs[nb]];
+            float m = 0.f;
+#pragma unroll
+            for (int l = 0; l < 3; l++)
+#pragma unroll
+                for (int nb = 0; nb < 27; nb++) m = fmaxf(m, fabsf(v[l][nb]));
+            const float sc = m + 1e-30f;
+            scale[r] = sc;
+            const float inv = 1.f / sc;
+            uint32_t pk[kMlpInPad / 2];
+#pragma unroll
+            for (int k = 0; k < kMlpInPad; k += 2) {
+                if (k < kMlpIn) {
+                    const float2 fv = mul2(make_float2(v[k / 27][k % 27], k + 1 < kMlpIn ? v[(k + 1) / 27][(k + 1) % 27] : 0.f),
+                                           make_float2(inv, inv));
+                    pk[k / 2] = pack_bf2(fv.x, fv.y);
+                } else {
+                    pk[k / 2] = 0u;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < kMlpInPad / 8; c++)
+                reinterpret_cast<uint4 *>(xr)[c] = make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
+        } else {
+            scale[r] = 1e-30f;
+#pragma unroll
+            for (int c = 0; c < kMlpInPad / 8; c++) reinterpret_cast<uint4 *>(xr)[c] = make_uint4(0, 0, 0, 0);
+        }
+        __syncwarp();
+        float yv[2][2];
+        forward_rows_regs(s, xs, w * 32, yv);
+        if (q == 0)
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int hrow = 0; hrow < 2; hrow++) {
+                    const int rr = w * 32 + mt * 16 + g + hrow * 8;
+                    const int64_t pr = a.pos[t * T + rr];
+                    if (pr >= 0) {
+                        const float vnew = scale[rr] * fminf(fmaxf(yv[mt][hrow], -1.f), 1.f);
+                        const int b = kPD + (rr / kFaceTU + 1) * kPU + (rr % kFaceTU + 1);
+                        a.corr[pr] = vnew - patch[b];  // minus p^{n+1} of the node (level 0)
+                    }
+                }
+    }
+}
+
 __global__ void k_abc_apply(const AbcArgs a, float *p_new)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x)
@@ -676,6 +806,7 @@ size_t smem_forward() { return sizeof(NetSmem) + sizeof(uint16_t) * T * (KP1 + K
 size_t smem_train() { return smem_forward() + sizeof(TrainSmem); }
 size_t smem_w3() { return smem_forward() + sizeof(float) * (T * H + T + H); }
 size_t smem_abc() { return kAbcXsOff + sizeof(uint16_t) * T * KP1 + sizeof(float) * T; }
+size_t smem_face() { return kFaceOffsOff + sizeof(int) * 32; }
 
 int grid_for(int64_t n)
 {
@@ -746,6 +877,20 @@ cudaError_t abc_correction(const MlpDev &net, const AbcArgs &a, cudaStream_t s)
     // persistent CTAs (four per SM fit the shared memory): the weights are staged once per CTA
     const int64_t tiles = (a.n + T - 1) / T;
     k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 152 * 4), T, sm, s>>>(net, a);
+    return cudaGetLastError();
+}
+
+cudaError_t abc_face(const MlpDev &net, const AbcFaceArgs &a, cudaStream_t s)
+{
+    if (a.ntiles <= 0) return cudaSuccess;
+    const size_t sm = smem_face();
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_abc_face, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_abc_face<<<(unsigned)std::min<int64_t>(a.ntiles, 152 * 4), T, sm, s>>>(net, a);
     return cudaGetLastError();
 }
 

@@ -42,6 +42,35 @@ struct AbcArgs {
     int absolute;          // 1: the network gives the node's value (scale * y), 0: a correction
 };
 
+// Face-tiled correction of the boundary nodes (strip layer 0): the six faces of the box are cut
+// into tiles of kFaceTU x kFaceTV nodes (one CTA tile of kMlpTile rows), every boundary node on
+// exactly one face.  A tile's three levels on the face plane and the plane inside it, with a
+// one-node rim, are staged in shared memory once, and each node's 81 features come from there.
+constexpr int kFaceTU = 16, kFaceTV = 8;
+static_assert(kFaceTU * kFaceTV == kMlpTile, "one face tile is one network tile");
+struct FaceDesc {
+    int axis_n, axis_u, axis_v;  // axes (0: x, 1: y, 2: z) normal to the face and along its tiles
+    int side;                    // node coordinate of the face along axis_n
+    int inward;                  // +1 or -1: the direction into the box along axis_n
+    int ulo, uhi, vlo, vhi;      // node ranges of the face along axis_u and axis_v
+};
+struct AbcFaceArgs {
+    FaceDesc face[6];
+    const int4 *tiles;     // (face, u0, v0, 0) per tile
+    int64_t ntiles;
+    const int64_t *pos;    // [ntiles * kMlpTile]: position of each tile row in the strip (-1: none)
+    const float *p_new;    // p^{n+1} (sponge applied)
+    const float *p_cur;    // p^n stored without its last sponge factor
+    const float *hist;     // p^{n-1} (actual values) on the two-node shell, device layout
+    float *hist_next;      // out: p^n (actual values) on the two-node shell, device layout
+    const float *sx, *sy, *sz;  // sponge factors (null: none)
+    int64_t nx, nxp, ny, nz;
+    float *corr;           // out: new value minus p^{n+1}, per strip position
+};
+// Face-tiled correction (the features, network, output and clipping of abc_correction with
+// absolute values), and p^n into hist_next on the shell.
+cudaError_t abc_face(const MlpDev &net, const AbcFaceArgs &a, cudaStream_t s);
+
 // bf16 conversion of the FP32 master weights into the device layout.
 cudaError_t mlp_pack(const float *master, uint16_t *w1, uint16_t *w2, float *b1, float *b2, float *w3, float *b3,
                      cudaStream_t s);

@@ -133,3 +133,38 @@ def test_trained_network_reduces_reflections(semgb_lib, cuda_device):
         e_net, _ = LB.reflected_energy(setup, net)
         print(f"reflected energy: sponge only {e_plain:.3e}, sponge + network {e_net:.3e}")
         assert e_net < bound * e_plain
+
+
+@pytest.mark.parametrize("sponge", [0, 2])
+def test_face_tiled_correction_matches_oracle(semgb_lib, cuda_device, sponge):
+    """Boundary nodes (layer 0) are corrected by the face-tiled kernel: each tile stages its three
+    levels on the face and the plane inside it once and builds every node's features from there,
+    and writes p^n of the two-node shell for the next step.  After 29 corrected steps and one
+    plain one, the correction equals the oracle network on the features the host gathers from the
+    same levels, every face (edges and corners included) is corrected, and nothing else changes."""
+    semgb = semgb_lib
+    from semgb import workloads as W
+    wl = W.small_random(9, 7, 8, 2, 30, seed=33, nsrc=1, nrec=4, sponge=sponge)
+    mesh, s = _solver(semgb, wl)
+    net = semgb.Mlp(0)
+    p = _params(10, 0.05)
+    net.params = p
+    abc = semgb.Abc(s, net, 0)
+    abc.step(29)
+    s.step(1)
+    x, sc = abc.features()
+    nodes = abc.nodes()
+    nx, ny, nz = wl.ex * 2 + 1, wl.ey * 2 + 1, wl.ez * 2 + 1
+    assert len(nodes) == nx * ny * nz - (nx - 2) * (ny - 2) * (nz - 2)
+    before = s.pressure()
+    abc.correct()
+    after = s.pressure()
+    yo, _ = M.forward(p, x)
+    want = sc * np.clip(yo, -1.0, 1.0)
+    got = after[nodes]
+    big = np.abs(want) > 1e-3 * np.abs(want).max()
+    assert big.sum() > 100
+    assert rel_l2(got[big], want[big]) < 5e-3
+    other = np.ones(mesh.n_nodes, bool)
+    other[nodes] = False
+    assert np.array_equal(after[other], before[other])
