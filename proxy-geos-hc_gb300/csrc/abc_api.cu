@@ -52,6 +52,10 @@ struct sem_abc {
     float *d_hist_alt = nullptr;
     int hcur = 0;
     FaceDesc faces[6];
+    // two corrected steps replayed as one CUDA graph, per (current level, history buffer)
+    // parity; valid while the solver's captured parameters are (graph_gen)
+    cudaGraphExec_t graph2[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    uint64_t graph_gen = 0;
     float *hist_now() const { return face && hcur ? d_hist_alt : d_hist; }
     float *hist_next() const { return face && !hcur ? d_hist_alt : d_hist; }
 };
@@ -296,7 +300,12 @@ int sem_mlp_train(sem_mlp *m, int64_t n, const float *x, const float *t, int epo
 int sem_abc_destroy(sem_abc *a)
 {
     if (!a) return SEM_OK;
-    if (a->s) cudaStreamSynchronize(a->s->stream);
+    // the solver may already be gone (handles closed in any order): wait for the device instead
+    // of the solver's stream
+    cudaDeviceSynchronize();
+    for (auto &row : a->graph2)
+        for (auto &g : row)
+            if (g) cudaGraphExecDestroy(g);
     dfree(a->d_nodes);
     dfree(a->d_shell);
     dfree(a->d_hist);
@@ -440,7 +449,39 @@ int sem_abc_step(sem_abc *a, int n_steps)
     if (s->kernel == SEM_KERNEL_ELEMENT) return sem_fail(SEM_ERR_STATE, "the learned boundary runs with the stencil pass");
     int rc = solver_prepare(s, n_steps);
     if (rc) return rc;
-    for (int k = 0; k < n_steps; k++) {
+    if (a->graph_gen != s->graph_gen) {
+        for (auto &row : a->graph2)
+            for (auto &g : row)
+                if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        a->graph_gen = s->graph_gen;
+    }
+    int done = 0;
+    while (n_steps - done >= 2) {
+        cudaGraphExec_t &ge = a->graph2[s->cur][a->hcur];
+        if (!ge) {
+            // capture two corrected steps; the level and history parities come back to where
+            // they started
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = cudaSuccess;
+            for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+                e = solver_enqueue_step(s, s->cur);
+                s->cur ^= 1;
+                if (e == cudaSuccess) e = enqueue_correction(a);
+            }
+            const cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return sem_fail(SEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+            }
+            const cudaError_t e3 = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            if (e3 != cudaSuccess) return sem_fail(SEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
+        }
+        CUDA_TRY(cudaGraphLaunch(ge, s->stream));
+        done += 2;
+    }
+    for (; done < n_steps; done++) {
         CUDA_TRY(solver_enqueue_step(s, s->cur));
         s->cur ^= 1;
         CUDA_TRY(enqueue_correction(a));

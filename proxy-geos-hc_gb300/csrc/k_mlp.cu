@@ -651,7 +651,7 @@ constexpr size_t kFaceXsOff = kAbcXsOff;
 constexpr size_t kFacePatchOff = kFaceXsOff + sizeof(uint16_t) * T * KP1 + sizeof(float) * T;
 constexpr size_t kFaceOffsOff = kFacePatchOff + sizeof(float) * 3 * kPL;
 
-__global__ void __launch_bounds__(128, 4) k_abc_face(const MlpDev net, const AbcFaceArgs a)
+__global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const AbcFaceArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
@@ -676,10 +676,12 @@ __global__ void __launch_bounds__(128, 4) k_abc_face(const MlpDev net, const Abc
             offs[threadIdx.x] = along(f.axis_n) * f.inward * kPD + along(f.axis_v) * kPU + along(f.axis_u);
         }
         // stage the face and inside planes of the three levels with a one-node rim; x-faces step
-        // through the depth fastest (adjacent in memory), the others along u (rows along x)
+        // through the depth fastest (adjacent in memory), the others along u (rows along x).  All
+        // of a thread's loads are issued first (one round trip), then stored.
         const bool depth_fast = f.axis_n == 0;
-        for (int i = threadIdx.x; i < 3 * 2 * kPD; i += blockDim.x) {
-            int l, di, vv, uu;
+        constexpr int NSTAGE = 3 * 2 * kPD, KS = (NSTAGE + T - 1) / T;
+        // element i of the patch: level, depth (1: face, 2: inside), position along v and u
+        auto decode = [&](int i, int &l, int &di, int &vv, int &uu) {
             if (depth_fast) {
                 di = i % 2 + 1;
                 const int r = i / 2;
@@ -689,31 +691,50 @@ __global__ void __launch_bounds__(128, 4) k_abc_face(const MlpDev net, const Abc
                 const int r = i / kPU;
                 vv = r % kPV; di = (r / kPV) % 2 + 1; l = r / (2 * kPV);
             }
+        };
+        // node coordinates by axis (selects, not an indexed array: they stay in registers)
+        auto coords = [&](int di, int vv, int uu, int &cx, int &cy, int &cz) {
             const int cu = u0 - 1 + uu, cv = v0 - 1 + vv, cn = f.side + (di - 1) * f.inward;
-            // node coordinates by axis (selects, not an indexed array: it stays in registers)
-            const int cx = f.axis_u == 0 ? cu : (f.axis_v == 0 ? cv : cn);
-            const int cy = f.axis_u == 1 ? cu : (f.axis_v == 1 ? cv : cn);
-            const int cz = f.axis_u == 2 ? cu : (f.axis_v == 2 ? cv : cn);
-            float val = 0.f;
-            const bool in = cx >= 0 && cx < a.nx && cy >= 0 && cy < a.ny && cz >= 0 && cz < a.nz;
-            if (in) {
-                const int64_t c[3] = {cx, cy, cz};
-                const int64_t qn = c[0] + c[2] * a.nxp + c[1] * plane;
-                if (l == 0) {
-                    val = a.p_new[qn];
-                } else if (l == 1) {
-                    val = a.p_cur[qn];
-                    if (a.sx) val = val * ((__ldg(a.sx + c[0]) * __ldg(a.sy + c[1])) * __ldg(a.sz + c[2]));
+            cx = f.axis_u == 0 ? cu : (f.axis_v == 0 ? cv : cn);
+            cy = f.axis_u == 1 ? cu : (f.axis_v == 1 ? cv : cn);
+            cz = f.axis_u == 2 ? cu : (f.axis_v == 2 ? cv : cn);
+        };
+        float sval[KS], sfac[KS];
+#pragma unroll
+        for (int k = 0; k < KS; k++) {
+            const int i = threadIdx.x + k * T;
+            sval[k] = 0.f;
+            sfac[k] = 1.f;
+            if (i < NSTAGE) {
+                int l, di, vv, uu, cx, cy, cz;
+                decode(i, l, di, vv, uu);
+                coords(di, vv, uu, cx, cy, cz);
+                if (cx >= 0 && cx < a.nx && cy >= 0 && cy < a.ny && cz >= 0 && cz < a.nz) {
+                    const int64_t qn = cx + (int64_t)cz * a.nxp + (int64_t)cy * plane;
+                    sval[k] = (l == 0 ? a.p_new : (l == 1 ? a.p_cur : a.hist))[qn];
+                    if (l == 1 && a.sx) sfac[k] = (__ldg(a.sx + cx) * __ldg(a.sy + cy)) * __ldg(a.sz + cz);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < KS; k++) {
+            const int i = threadIdx.x + k * T;
+            if (i < NSTAGE) {
+                int l, di, vv, uu, cx, cy, cz;
+                decode(i, l, di, vv, uu);
+                float val = sval[k];
+                if (l == 1) {
+                    val = val * sfac[k];  // p^n is stored without its last sponge factor
                     // p^n of the tile's own nodes and their inside neighbours: the next step's
                     // p^{n-1} (every node of the two-node shell is one of these for some tile)
                     const int us = u0 - 1 + uu, vs = v0 - 1 + vv;
-                    if (uu >= 1 && uu <= kFaceTU && vv >= 1 && vv <= kFaceTV && us < f.uhi && vs < f.vhi)
-                        a.hist_next[qn] = val;
-                } else {
-                    val = a.hist[qn];
+                    if (uu >= 1 && uu <= kFaceTU && vv >= 1 && vv <= kFaceTV && us < f.uhi && vs < f.vhi) {
+                        coords(di, vv, uu, cx, cy, cz);
+                        a.hist_next[cx + (int64_t)cz * a.nxp + (int64_t)cy * plane] = val;
+                    }
                 }
+                patch[l * kPL + di * kPD + vv * kPU + uu] = val;
             }
-            patch[l * kPL + di * kPD + vv * kPU + uu] = val;
         }
         __syncthreads();
         // features of the row's node from the patch (as k_abc_correction gathers them)
@@ -890,7 +911,18 @@ cudaError_t abc_face(const MlpDev &net, const AbcFaceArgs &a, cudaStream_t s)
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_abc_face<<<(unsigned)std::min<int64_t>(a.ntiles, 152 * 4), T, sm, s>>>(net, a);
+    // persistent CTAs, as many as are resident at once (the weights are staged once per CTA)
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_abc_face, T, sm) != cudaSuccess || per_sm < 1) {
+            cudaGetLastError();
+            per_sm = 1;
+        }
+    }
+    k_abc_face<<<(unsigned)std::min<int64_t>(a.ntiles, (int64_t)sms * per_sm), T, sm, s>>>(net, a);
     return cudaGetLastError();
 }
 
