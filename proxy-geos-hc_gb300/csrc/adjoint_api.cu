@@ -37,6 +37,12 @@ struct sem_adjoint {
     float *d_ckpt = nullptr;    // [nseg][2][n_int]: current and stored previous level at n = seg*every
     float *d_kp = nullptr;      // [every][n_int]: K p' of the steps of one segment
     float *d_grad = nullptr;    // [n_int]
+    int *d_seg = nullptr;       // segment the backward sweep is on (read by its graphs)
+    // one backward segment of `every` steps (restore, recompute, adjoint) replayed as a CUDA
+    // graph, per (forward, adjoint) level parity at its start; valid while both solvers'
+    // captured parameters are (gen)
+    cudaGraphExec_t seg_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    uint64_t seg_gen[2] = {0, 0};
     int64_t n_int = 0;
     bool have_forward = false;
     int nrec = 0;
@@ -47,10 +53,61 @@ struct sem_adjoint {
 
 namespace {
 
-__global__ void k_set_ctr(int *ctr, int n)
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
+__global__ void k_dec_int(int *p) { *p -= 1; }
+
+// Levels of the forward run at the start of segment *seg (its checkpoint) and the step counter
+__global__ void k_restore_segment(const float *ckpt, const int *seg, int64_t lv, int every, float *cur, float *prev,
+                                  int *ctr)
 {
-    ctr[0] = n;
-    ctr[1] = n - 1;
+    const int sg = *seg;
+    const float *ck = ckpt + (size_t)sg * 2 * lv;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < lv / 4; i += (int64_t)gridDim.x * blockDim.x) {
+        reinterpret_cast<float4 *>(cur)[i] = reinterpret_cast<const float4 *>(ck)[i];
+        reinterpret_cast<float4 *>(prev)[i] = reinterpret_cast<const float4 *>(ck + lv)[i];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctr[0] = sg * every;
+        ctr[1] = sg * every - 1;
+    }
+}
+
+void destroy_seg_graphs(sem_adjoint *a)
+{
+    for (auto &row : a->seg_graph)
+        for (auto &g : row)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+// One backward segment of `len` steps, the segment index read from the device: restore its
+// checkpoint, recompute it recording K p', run its adjoint steps newest first with the gradient,
+// then step the segment index down.
+cudaError_t enqueue_segment(sem_adjoint *a, int len)
+{
+    sem_solver *f = a->fwd, *g = a->adj;
+    const size_t lv = (size_t)a->n_int;
+    cudaError_t e;
+    k_restore_segment<<<152 * 8, 256, 0, f->stream>>>(a->d_ckpt, a->d_seg, a->n_int, a->every, f->d_p[f->cur],
+                                                        f->d_p[1 - f->cur], f->d_ctr);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    for (int n = 0; n < len; n++) {
+        StepExtra x;
+        x.mode = STENCIL_RECORD_KP;
+        x.kp = a->d_kp + (size_t)n * lv;
+        if ((e = solver_enqueue_step(f, f->cur, nullptr, &x)) != cudaSuccess) return e;
+        f->cur ^= 1;
+    }
+    for (int n = len - 1; n >= 0; n--) {
+        StepExtra x;
+        x.mode = STENCIL_GRADIENT;
+        x.kp = a->d_kp + (size_t)n * lv;
+        x.grad = a->d_grad;
+        if ((e = solver_enqueue_step(g, g->cur, nullptr, &x)) != cudaSuccess) return e;
+        g->cur ^= 1;
+    }
+    k_dec_int<<<1, 1, 0, f->stream>>>(a->d_seg);
+    return cudaGetLastError();
 }
 
 int check_ready(const sem_adjoint *a)
@@ -67,6 +124,8 @@ int sem_adjoint_destroy(sem_adjoint *a)
 {
     if (!a) return SEM_OK;
     if (a->fwd) cudaStreamSynchronize(a->fwd->stream);
+    destroy_seg_graphs(a);
+    dfree(a->d_seg);
     if (a->adj) sem_solver_destroy(a->adj);
     if (a->fwd) sem_solver_destroy(a->fwd);
     dfree(a->d_ckpt);
@@ -102,7 +161,7 @@ int sem_adjoint_create(sem_mesh *m, float dt, int n_steps, int checkpoint_every,
     cudaError_t e;
     if ((e = dalloc(&a->d_ckpt, (size_t)a->nseg * 2 * a->n_int)) != cudaSuccess ||
         (e = dalloc(&a->d_kp, (size_t)a->every * a->n_int)) != cudaSuccess ||
-        (e = dalloc(&a->d_grad, (size_t)a->n_int)) != cudaSuccess) {
+        (e = dalloc(&a->d_grad, (size_t)a->n_int)) != cudaSuccess || (e = dalloc(&a->d_seg, 1)) != cudaSuccess) {
         sem_adjoint_destroy(a);
         return sem_fail(SEM_ERR_OOM, std::string("checkpoint storage: ") + cudaGetErrorString(e));
     }
@@ -248,26 +307,37 @@ int sem_adjoint_backward(sem_adjoint *a, const float *residual, float *grad)
     if ((rc = solver_prepare(g, N)) != SEM_OK) return rc;
     if ((rc = solver_prepare(f, 0)) != SEM_OK) return rc;
     CUDA_TRY(cudaMemsetAsync(a->d_grad, 0, lv * 4, f->stream));
-    for (int seg = a->nseg - 1; seg >= 0; seg--) {
-        const int n0 = seg * a->every, n1 = std::min(n0 + a->every, N);
-        const float *ck = a->d_ckpt + (size_t)seg * 2 * lv;
-        CUDA_TRY(cudaMemcpyAsync(f->d_p[f->cur], ck, lv * 4, cudaMemcpyDeviceToDevice, f->stream));
-        CUDA_TRY(cudaMemcpyAsync(f->d_p[1 - f->cur], ck + lv, lv * 4, cudaMemcpyDeviceToDevice, f->stream));
-        k_set_ctr<<<1, 1, 0, f->stream>>>(f->d_ctr, n0);
-        CUDA_TRY(cudaGetLastError());
-        for (int n = n0; n < n1; n++) {
-            StepExtra x;
-            x.mode = STENCIL_RECORD_KP;
-            x.kp = a->d_kp + (size_t)(n - n0) * lv;
-            CUDA_TRY(solver_enqueue_step(f, f->cur, nullptr, &x));
-            f->cur ^= 1;
+    if (a->seg_gen[0] != f->graph_gen || a->seg_gen[1] != g->graph_gen) {
+        destroy_seg_graphs(a);
+        a->seg_gen[0] = f->graph_gen;
+        a->seg_gen[1] = g->graph_gen;
+    }
+    k_set_int<<<1, 1, 0, f->stream>>>(a->d_seg, a->nseg - 1);
+    CUDA_TRY(cudaGetLastError());
+    // the newest segment (possibly shorter) directly, then whole segments from graphs
+    CUDA_TRY(enqueue_segment(a, N - (a->nseg - 1) * a->every));
+    for (int seg = a->nseg - 2; seg >= 0; seg--) {
+        cudaGraphExec_t &ge = a->seg_graph[f->cur][g->cur];
+        if (!ge) {
+            cudaGraph_t gr = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal));
+            const int fc = f->cur, gc = g->cur;
+            const cudaError_t e1 = enqueue_segment(a, a->every);
+            const cudaError_t e2 = cudaStreamEndCapture(f->stream, &gr);
+            // the capture ran nothing: the parities advance with the replays below
+            f->cur = fc;
+            g->cur = gc;
+            if (e1 != cudaSuccess || e2 != cudaSuccess) {
+                if (gr) cudaGraphDestroy(gr);
+                return sem_fail(SEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+            }
+            const cudaError_t e3 = cudaGraphInstantiate(&ge, gr, 0);
+            cudaGraphDestroy(gr);
+            if (e3 != cudaSuccess) return sem_fail(SEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
         }
-        for (int n = n1 - 1; n >= n0; n--) {
-            StepExtra x;
-            x.mode = STENCIL_GRADIENT;
-            x.kp = a->d_kp + (size_t)(n - n0) * lv;
-            x.grad = a->d_grad;
-            CUDA_TRY(solver_enqueue_step(g, g->cur, nullptr, &x));
+        CUDA_TRY(cudaGraphLaunch(ge, f->stream));
+        if (a->every % 2) {
+            f->cur ^= 1;
             g->cur ^= 1;
         }
     }
