@@ -518,8 +518,9 @@ def measure_batched(steps: int = 40, n: int = 100, shots: int = 64):
 
 def measure_uneven(steps: int = 20, lo: int = 40, hi: int = 120, name: str = "c3_uneven_32"):
     """32 independent problems (per-axis elements in [lo, hi], orders {2, 3, 4}) advanced as one
-    group (one multi-branch CUDA graph per two steps) against the same solvers stepped one after
-    another: node-steps/s over the whole batch."""
+    group -- one launch per step over every member's tiles (the default), and each member's own
+    launches as branches of one graph -- against the same solvers stepped one after another:
+    node-steps/s over the whole batch."""
     import torch
     import semgb
     from semgb import workloads as W
@@ -531,20 +532,29 @@ def measure_uneven(steps: int = 20, lo: int = 40, hi: int = 120, name: str = "c3
         s.set_stream(stream.cuda_stream)
         s.step(2)
     seq_ms = _ev_time(stream, lambda: [s.step(steps) for _, s in members])
-    g = semgb.Group([s for _, s in members])
-    g.step(2)
-    g.synchronize()
-    grp_ms = g.time_step(steps) * steps
-    g.synchronize()
-    g.close()
+    res = {}
+    for form in (semgb.GROUP_ONE_LAUNCH, semgb.GROUP_BRANCHES):
+        g = semgb.Group([s for _, s in members], launch=form)
+        g.step(2)
+        g.synchronize()
+        ms = g.time_step(steps) * steps
+        g.synchronize()
+        res[form] = (ms, g.launch)
+        g.close()
     for m, s in members:
         s.close()
         m.close()
+    one_ms, one_form = res[semgb.GROUP_ONE_LAUNCH]
+    br_ms, _ = res[semgb.GROUP_BRANCHES]
     return {"workload": name, "problems": len(wls), "elements_per_axis": [lo, hi], "nodes": nodes, "steps": steps,
             "orders": sorted({w.order for w in wls}),
-            "group_Gnode_steps_per_s": nodes * steps / (grp_ms / 1e3) / 1e9,
+            "one_launch": one_form == semgb.GROUP_ONE_LAUNCH,
+            "launches_per_step": 2 if one_form == semgb.GROUP_ONE_LAUNCH else 2 * len(wls),
+            "group_Gnode_steps_per_s": nodes * steps / (one_ms / 1e3) / 1e9,
+            "branches_Gnode_steps_per_s": nodes * steps / (br_ms / 1e3) / 1e9,
             "sequential_Gnode_steps_per_s": nodes * steps / (seq_ms / 1e3) / 1e9,
-            "speedup_vs_sequential": seq_ms / grp_ms}
+            "speedup_vs_sequential": seq_ms / one_ms,
+            "branches_speedup_vs_sequential": seq_ms / br_ms}
 
 
 def measure_adjoint(shots: int = 16, fd_dirs: int = 8, n: int = 96, steps: int = 2000):

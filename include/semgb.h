@@ -297,16 +297,26 @@ int sem_batch_autotune(sem_batch *b, int *shots_per_cluster, int *warps_per_cta,
 /* ------------------------------------------------------------------------------------------
  * Groups of independent problems of uneven size (different meshes, orders, models, dt).  The
  * reference runs one problem per process (SEMproxy.cpp:41-64); a group advances several
- * solvers together, replaying one CUDA graph per two steps that holds every member's steps as
- * a parallel branch, so small members fill the SMs that large ones leave idle.  Members keep
- * their own state and I/O (sem_solver_get_traces etc.); they use the stencil pass.  A solver
- * belongs to at most one group at a time; the group must be destroyed before its members.
+ * solvers together, replaying one CUDA graph per two steps.  Two launch forms:
+ *   SEM_GROUP_ONE_LAUNCH (default): each step is one source launch and one stencil-pass launch
+ *     whose CTAs cover every member's tiles, so small members fill the SMs that large ones
+ *     leave idle within the launch.  Needs every member on the stencil pass with order <= 4,
+ *     the direct form and the default rounding; otherwise the group uses the branches.
+ *   SEM_GROUP_BRANCHES: each member's own launches as a parallel branch of the graph.
+ * Members keep their own state and I/O (sem_solver_get_traces etc.) and give the same bits as
+ * when stepped alone; they may be stepped alone between group steps.  A solver belongs to at
+ * most one group at a time; the group must be destroyed before its members.
  * ------------------------------------------------------------------------------------------ */
 
 typedef struct sem_group sem_group;
+enum { SEM_GROUP_ONE_LAUNCH = 0, SEM_GROUP_BRANCHES = 1 };
 
 int sem_group_create(int n_solvers, sem_solver *const *solvers, sem_group **out);
 int sem_group_destroy(sem_group *g);
+/* Requested launch form (SEM_GROUP_*), from the next step on. */
+int sem_group_set_launch(sem_group *g, int form);
+/* Launch form of the last step (before any step: the requested one). */
+int sem_group_get_launch(sem_group *g, int *form);
 /* Every member advances n_steps (enqueued; ordered after earlier work on the members' streams
  * and before later calls on them). */
 int sem_group_step(sem_group *g, int n_steps);

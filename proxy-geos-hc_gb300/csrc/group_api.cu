@@ -1,12 +1,15 @@
 // group_api.cu -- many independent problems of uneven size advanced together (sem_group_*).
 //
 // Each member is an ordinary solver (its own mesh, order, model, dt, sources and receivers).
-// The group captures one CUDA graph per two steps with one branch per member: the group stream
-// forks into the members' streams, each branch holds that member's two steps (source, stencil
-// pass with update and receivers), and the branches join back.  A launch of the graph hands all
-// members' kernels to the GPU at once, so small problems fill the SMs that large ones leave idle
-// and the host issues one launch per two steps for the whole group.  Branches are captured
-// largest member first.
+// Two ways to advance them, both replayed from one CUDA graph per two steps:
+//  - one launch (default where every member allows it: stencil pass, orders 1-4, direct form,
+//    default rounding): per step one source launch and one pass launch over all members' CTAs
+//    (k_group.cu).  The members' tiles are cut along y into chunks of about the same number of
+//    planes, chosen for the whole group, and the longest CTAs come first in the launch;
+//  - branches: the group stream forks into the members' streams, each branch holds that member's
+//    own steps (source, stencil pass), and the branches join back; largest member first.
+// Each member's results are bit for bit those of the member stepped alone, either way.  Members
+// may also be stepped alone between group steps: the group follows each member's current level.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -16,14 +19,27 @@
 #include "abi.h"
 #include "solver.h"
 
+using semgb::Box;
+using semgb::GroupMember;
+using semgb::StencilTables;
+
 struct sem_group {
     std::vector<sem_solver *> members;  // capture order: largest first
     cudaStream_t stream = nullptr;
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> join;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [0]: levels as at capture, [1]: after an odd step
-    std::vector<uint64_t> gen;                      // members' graph generations at capture
-    int flip = 0;                                   // parity of the members' levels against the capture
+    int want = SEM_GROUP_ONE_LAUNCH;   // requested launch form
+    int form = -1;                     // form of the graphs and state below
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [f]: two steps starting at parity f
+    std::vector<uint64_t> gen;         // members' graph generations at build
+    std::vector<int> cur0;             // member's current level at parity 0
+    int flip = 0;                      // parity of the next step
+    // one-launch form
+    std::vector<StencilTables *> tabs;  // the members' tables with the group's y-chunks
+    std::vector<float *> ones;          // unit sponge factors of members without a sponge
+    GroupMember *d_mem = nullptr;
+    int *d_cta_member = nullptr;
+    int n_ctas = 0, max_order = 0;
 };
 
 namespace {
@@ -32,8 +48,18 @@ void drop_graphs(sem_group *g)
 {
     for (auto &x : g->graph)
         if (x) { cudaGraphExecDestroy(x); x = nullptr; }
-    g->gen.clear();
-    g->flip = 0;
+}
+
+void free_one_launch(sem_group *g)
+{
+    for (auto &t : g->tabs) semgb::stencil_tables_free(t);
+    g->tabs.clear();
+    for (float *p : g->ones)
+        if (p) cudaFree(p);
+    g->ones.clear();
+    if (g->d_mem) { cudaFree(g->d_mem); g->d_mem = nullptr; }
+    if (g->d_cta_member) { cudaFree(g->d_cta_member); g->d_cta_member = nullptr; }
+    g->n_ctas = 0;
 }
 
 bool stale(const sem_group *g)
@@ -44,15 +70,27 @@ bool stale(const sem_group *g)
     return false;
 }
 
-// Fork the members from the group stream, enqueue `steps` steps on each, join them back.
-cudaError_t enqueue_all(sem_group *g, int steps)
+bool one_launch_allowed(const sem_group *g)
+{
+    for (const sem_solver *s : g->members) {
+        const int o = s->mesh->box.order;
+        if (s->kernel == SEM_KERNEL_ELEMENT || o > semgb::kGroupMaxOrder || s->form != SEM_FORM_DIRECT ||
+            s->rounding != SEM_ROUNDING_DEFAULT || !s->stencil || s->stencil->nshot != 1)
+            return false;
+    }
+    return true;
+}
+
+// Fork the members from the group stream, enqueue `steps` steps on each from level
+// cur0 ^ parity, join them back.
+cudaError_t enqueue_branches(sem_group *g, int steps, int parity)
 {
     cudaError_t e = cudaEventRecord(g->fork, g->stream);
     if (e != cudaSuccess) return e;
     for (size_t i = 0; i < g->members.size(); i++) {
         sem_solver *s = g->members[i];
         if ((e = cudaStreamWaitEvent(s->stream, g->fork, 0)) != cudaSuccess) return e;
-        int c = s->cur;
+        int c = g->cur0[i] ^ parity;
         for (int k = 0; k < steps; k++, c ^= 1)
             if ((e = solver_enqueue_step(s, c)) != cudaSuccess) return e;
         if ((e = cudaEventRecord(g->join[i], s->stream)) != cudaSuccess) return e;
@@ -61,21 +99,168 @@ cudaError_t enqueue_all(sem_group *g, int steps)
     return cudaSuccess;
 }
 
-int capture(sem_group *g, int which)
+cudaError_t enqueue_one_launch(sem_group *g, int steps, int parity)
+{
+    for (int k = 0; k < steps; k++) {
+        cudaError_t e = semgb::launch_group_step(g->d_mem, (int)g->members.size(), g->d_cta_member, g->n_ctas,
+                                                 g->max_order, parity ^ (k & 1), g->stream);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t enqueue(sem_group *g, int steps, int parity)
+{
+    return g->form == SEM_GROUP_ONE_LAUNCH ? enqueue_one_launch(g, steps, parity) : enqueue_branches(g, steps, parity);
+}
+
+int capture(sem_group *g, int parity)
 {
     cudaGraph_t graph = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e1 = enqueue_all(g, 2);
+    cudaError_t e1 = enqueue(g, 2, parity);
     cudaError_t e2 = cudaStreamEndCapture(g->stream, &graph);
     if (e1 != cudaSuccess || e2 != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         return sem_fail(SEM_ERR_CUDA, std::string("group graph capture: ") +
                                           cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
     }
-    cudaError_t e3 = cudaGraphInstantiate(&g->graph[which], graph, 0);
+    cudaError_t e3 = cudaGraphInstantiate(&g->graph[parity], graph, 0);
     cudaGraphDestroy(graph);
     if (e3 != cudaSuccess) return sem_fail(SEM_ERR_CUDA, cudaGetErrorString(e3));
     return SEM_OK;
+}
+
+// y-chunk length of every member for one launch over the group: chunks of about L planes, L
+// chosen to minimise max(total work / resident CTAs, longest CTA), the work of a CTA being its
+// planes plus the 2o planes it reads before its first output (longest CTAs run first, so the
+// last wave is no longer than the longest CTA).
+std::vector<int> group_chunks(const sem_group *g, int64_t resident)
+{
+    const size_t n = g->members.size();
+    int64_t ny_max = 1;
+    for (const sem_solver *s : g->members) ny_max = std::max(ny_max, s->mesh->box.ny);
+    double best = 1e300;
+    int64_t best_l = ny_max;
+    for (int64_t L = 1; L <= ny_max; L++) {
+        double work = 0, longest = 0;
+        for (const sem_solver *s : g->members) {
+            const Box &b = s->mesh->box;
+            const int64_t cols = (int64_t)s->stencil->grid[0] * s->stencil->grid[1];
+            const int64_t c = (b.ny + L - 1) / L, chunk = (b.ny + c - 1) / c;
+            work += (double)cols * c * (chunk + 2 * b.order);
+            longest = std::max(longest, (double)(chunk + 2 * b.order));
+        }
+        const double cost = std::max(work / (double)resident, longest);
+        if (cost < best - 1e-9) { best = cost; best_l = L; }
+    }
+    std::vector<int> out(n);
+    for (size_t i = 0; i < n; i++) {
+        const int64_t ny = g->members[i]->mesh->box.ny;
+        const int64_t c = (ny + best_l - 1) / best_l;
+        out[i] = (int)((ny + c - 1) / c);
+    }
+    return out;
+}
+
+// Member descriptors from the members' current state (levels cur0 ^ k at parity k).
+int write_descriptors(sem_group *g)
+{
+    const size_t n = g->members.size();
+    std::vector<GroupMember> h(n);
+    int cta = 0;
+    // launch order: longest CTAs first
+    std::vector<size_t> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return g->tabs[a]->ychunk + 2 * g->tabs[a]->order > g->tabs[b]->ychunk + 2 * g->tabs[b]->order;
+    });
+    std::vector<int> cta_member;
+    for (size_t oi = 0; oi < n; oi++) {
+        const size_t i = order[oi];
+        sem_solver *s = g->members[i];
+        const StencilTables &t = *g->tabs[i];
+        GroupMember &m = h[i];
+        m.t = t;
+        m.t.class_tab = nullptr;
+        m.order = t.order;
+        m.cur0 = g->cur0[i];
+        m.cta0 = cta;
+        const float *ones = g->ones[i];
+        for (int k = 0; k < 2; k++) {
+            const int c = g->cur0[i] ^ k;
+            semgb::StencilArgs &a = m.a[k];
+            a = semgb::StencilArgs{};
+            a.cur = s->d_p[c];
+            a.prev = s->d_p[1 - c];
+            a.sx = s->sponge ? s->d_sx : ones;
+            a.sy = s->sponge ? s->d_sy : ones;
+            a.sz = s->sponge ? s->d_sz : ones;
+            a.status = s->d_status;
+            a.rec_node = s->d_rec_node;
+            a.rec_perm = s->d_rec_perm;
+            a.rec_off = t.d_rec_off;
+            a.rec_idx = t.d_rec_idx;
+            a.nrec = s->nrec;
+            a.traces = s->d_traces;
+            a.ctr = s->d_ctr;
+            m.src[k] = semgb::SourceArgs{s->d_p[c], s->d_src_node, s->d_src_coef, s->d_wavelet,
+                                         s->nsamples > 0 ? s->nsrc : 0, s->nsamples, s->d_ctr, s->src_distinct ? 1 : 0};
+        }
+        const int64_t nc = (int64_t)t.grid[0] * t.grid[1] * t.grid[2];
+        if (cta + nc > (int64_t)0x7fffffff) return sem_fail(SEM_ERR_ARG, "group too large for one launch");
+        cta_member.insert(cta_member.end(), (size_t)nc, (int)i);
+        cta += (int)nc;
+    }
+    if (!g->d_mem) {
+        CUDA_TRY(cudaMalloc(&g->d_mem, n * sizeof(GroupMember)));
+        CUDA_TRY(cudaMalloc(&g->d_cta_member, cta_member.size() * sizeof(int)));
+    } else if ((int)cta_member.size() != g->n_ctas) {
+        return sem_fail(SEM_ERR_STATE, "group launch changed size");
+    }
+    g->n_ctas = (int)cta_member.size();
+    // the group stream is idle here (callers synchronise it first), so plain copies are ordered
+    CUDA_TRY(cudaMemcpy(g->d_mem, h.data(), n * sizeof(GroupMember), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(g->d_cta_member, cta_member.data(), cta_member.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return SEM_OK;
+}
+
+// Tables, unit sponges and descriptors of the one-launch form from the members' current state.
+int build_one_launch(sem_group *g)
+{
+    CUDA_TRY(cudaStreamSynchronize(g->stream));  // no launch of the group still reads the old state
+    CUDA_TRY(semgb::group_kernel_setup());
+    const size_t n = g->members.size();
+    int max_order = 1;
+    for (const sem_solver *s : g->members) max_order = std::max(max_order, s->mesh->box.order);
+    int dev = 0, sms = 152;
+    CUDA_TRY(cudaGetDevice(&dev));
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int per_sm = std::max(1, semgb::group_blocks_per_sm(max_order));
+    const std::vector<int> chunks = group_chunks(g, (int64_t)sms * per_sm);
+    for (auto &t : g->tabs) semgb::stencil_tables_free(t);
+    g->tabs.assign(n, nullptr);
+    if (g->ones.size() != n) g->ones.assign(n, nullptr);
+    for (size_t i = 0; i < n; i++) {
+        sem_solver *s = g->members[i];
+        StencilTables *t = new StencilTables(*s->stencil);  // tensor maps of the member's levels
+        t->class_tab = nullptr;
+        t->d_rec_off = nullptr;
+        t->d_rec_idx = nullptr;
+        t->ychunk = chunks[i];
+        t->grid[2] = (int)((t->ny + chunks[i] - 1) / chunks[i]);
+        g->tabs[i] = t;
+        CUDA_TRY(semgb::stencil_set_receivers(*t, s->rec_sorted.data(), s->nrec, s->rec_version));
+        if (!s->sponge && !g->ones[i]) {
+            const Box &b = s->mesh->box;
+            const size_t len = (size_t)std::max(b.nx, std::max(b.ny, b.nz));
+            std::vector<float> one(len, 1.f);
+            CUDA_TRY(cudaMalloc(&g->ones[i], len * sizeof(float)));
+            CUDA_TRY(cudaMemcpy(g->ones[i], one.data(), len * sizeof(float), cudaMemcpyHostToDevice));
+        }
+    }
+    g->max_order = max_order;
+    return write_descriptors(g);
 }
 
 }  // namespace
@@ -87,6 +272,7 @@ int sem_group_destroy(sem_group *g)
     if (!g) return SEM_OK;
     if (g->stream) cudaStreamSynchronize(g->stream);
     drop_graphs(g);
+    free_one_launch(g);
     for (auto e : g->join) cudaEventDestroy(e);
     if (g->fork) cudaEventDestroy(g->fork);
     if (g->stream) cudaStreamDestroy(g->stream);
@@ -121,6 +307,24 @@ int sem_group_create(int n, sem_solver *const *solvers, sem_group **out)
     GUARD_END
 }
 
+int sem_group_set_launch(sem_group *g, int form)
+{
+    GUARD_BEGIN
+    if (!g || (form != SEM_GROUP_ONE_LAUNCH && form != SEM_GROUP_BRANCHES)) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    g->want = form;
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_group_get_launch(sem_group *g, int *form)
+{
+    GUARD_BEGIN
+    if (!g || !form) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    *form = g->form >= 0 ? g->form : g->want;
+    return SEM_OK;
+    GUARD_END
+}
+
 int sem_group_step(sem_group *g, int n_steps)
 {
     GUARD_BEGIN
@@ -131,13 +335,34 @@ int sem_group_step(sem_group *g, int n_steps)
         int rc = solver_prepare(s, n_steps);
         if (rc) return rc;
     }
-    if (stale(g)) {
+    const size_t n = g->members.size();
+    const int form = g->want == SEM_GROUP_ONE_LAUNCH && one_launch_allowed(g) ? SEM_GROUP_ONE_LAUNCH : SEM_GROUP_BRANCHES;
+    bool rebuild = stale(g) || form != g->form;
+    if (!rebuild) {
+        // members stepped alone since the last group step: follow their current levels
+        for (size_t i = 0; i < n && !rebuild; i++)
+            if ((g->cur0[i] ^ g->flip) != g->members[i]->cur) rebuild = true;
+    }
+    if (rebuild) {
+        CUDA_TRY(cudaStreamSynchronize(g->stream));
         drop_graphs(g);
-        g->gen.resize(g->members.size());
-        for (size_t i = 0; i < g->members.size(); i++) g->gen[i] = g->members[i]->graph_gen;
+        g->form = form;
+        g->flip = 0;
+        g->cur0.resize(n);
+        g->gen.resize(n);
+        for (size_t i = 0; i < n; i++) {
+            g->cur0[i] = g->members[i]->cur;
+            g->gen[i] = g->members[i]->graph_gen;
+        }
+        if (form == SEM_GROUP_ONE_LAUNCH) {
+            int rc = build_one_launch(g);
+            if (rc) return rc;
+        } else {
+            free_one_launch(g);
+        }
     }
     // order against work already on the members' own streams (set-up, earlier solo steps)
-    for (size_t i = 0; i < g->members.size(); i++) {
+    for (size_t i = 0; i < n; i++) {
         CUDA_TRY(cudaEventRecord(g->join[i], g->members[i]->stream));
         CUDA_TRY(cudaStreamWaitEvent(g->stream, g->join[i], 0));
     }
@@ -151,7 +376,7 @@ int sem_group_step(sem_group *g, int n_steps)
         done += 2;
     }
     if (done < n_steps) {
-        CUDA_TRY(enqueue_all(g, 1));
+        CUDA_TRY(enqueue(g, 1, g->flip));
         for (sem_solver *s : g->members) s->cur ^= 1;
         g->flip ^= 1;
     }

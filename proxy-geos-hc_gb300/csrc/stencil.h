@@ -80,6 +80,30 @@ struct StencilArgs {
 
 enum StencilMode { STENCIL_PLAIN = 0, STENCIL_RECORD_KP = 1, STENCIL_GRADIENT = 2 };
 
+// One member of a group launch (k_group.cu): several boxes of orders 1..kGroupMaxOrder advanced
+// by one launch per step.  Lives in device memory; the launch's CTAs cta0.. belong to it.
+constexpr int kGroupMaxOrder = 4;
+struct alignas(64) GroupMember {
+    StencilTables t;    // tensor maps of the member's levels, its tiling with the group's y-chunks
+    StencilArgs a[2];   // [k]: pass arguments at group parity k (current level cur0 ^ k)
+    SourceArgs src[2];  // [k]: source arguments at group parity k
+    int order;
+    int cur0;           // index of the member's current level at parity 0
+    int cta0;           // the member's first CTA in the launch
+};
+
+// Set up the group kernels on the current device (coefficient tables, shared-memory limit).
+cudaError_t group_kernel_setup();
+// Dynamic shared memory of a group launch whose members have orders up to max_order, and the
+// CTAs per SM it allows (threads per CTA: kGroupThreads).
+constexpr int kGroupThreads = 128;
+size_t group_smem(int max_order);
+int group_blocks_per_sm(int max_order);
+// One step of every member: sources, then the pass (receivers included).  cta_member[c] is the
+// member of CTA c; members[m].cta0 its first CTA.
+cudaError_t launch_group_step(const GroupMember *members, int n_members, const int *cta_member, int n_ctas,
+                              int max_order, int k, cudaStream_t s);
+
 // Tables and tiling for a box (no device buffers yet).  Returns 0 or a cudaError_t.
 // nshot > 1: the many-shot form, levels holding nshot fields one after another (traces
 // [step][receiver][shot]); dt^2/M and the sponge are shared.

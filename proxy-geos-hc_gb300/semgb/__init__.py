@@ -22,6 +22,7 @@ SEM_OK, SEM_ERR_ARG, SEM_ERR_CUDA, SEM_ERR_OOM, SEM_ERR_TIMEOUT, SEM_ERR_UNSTABL
 KERNEL_AUTO, KERNEL_ELEMENT, KERNEL_STENCIL = 0, 1, 2
 FORM_DIRECT, FORM_DIFFERENCE = 0, 1
 ROUNDING_DEFAULT, ROUNDING_REFERENCE = 0, 1
+GROUP_ONE_LAUNCH, GROUP_BRANCHES = 0, 1
 LEVEL_CURRENT, LEVEL_PREVIOUS = 0, 1
 
 _I64P = C.POINTER(C.c_int64)
@@ -122,6 +123,8 @@ _SIGS = {
     "sem_group_step": [_VP, C.c_int],
     "sem_group_synchronize": [_VP],
     "sem_group_time_step": [_VP, C.c_int, C.POINTER(C.c_float)],
+    "sem_group_set_launch": [_VP, C.c_int],
+    "sem_group_get_launch": [_VP, C.POINTER(C.c_int)],
     "sem_adjoint_create": [_VP, C.c_float, C.c_int, C.c_int, C.POINTER(_VP)],
     "sem_adjoint_destroy": [_VP],
     "sem_adjoint_set_sponge": [_VP, C.c_int, C.c_float],
@@ -520,15 +523,25 @@ class Batch:
 
 
 class Group:
-    """Independent solvers of uneven size advanced together (sem_group_*); one CUDA graph per
-    two steps holds every member's steps as a parallel branch."""
+    """Independent solvers of uneven size advanced together (sem_group_*), one CUDA graph per
+    two steps: by default one launch per step over every member's tiles (GROUP_ONE_LAUNCH),
+    or each member's own launches as parallel branches (GROUP_BRANCHES)."""
 
-    def __init__(self, solvers):
+    def __init__(self, solvers, launch: int = 0):
         self.solvers = list(solvers)  # keeps the members alive while the group exists
         arr = (_VP * len(self.solvers))(*[s._h for s in self.solvers])
         h = _VP()
         _check(lib().sem_group_create(len(self.solvers), arr, C.byref(h)))
         self._h = h
+        if launch != GROUP_ONE_LAUNCH:
+            _check(lib().sem_group_set_launch(self._h, launch))
+
+    @property
+    def launch(self) -> int:
+        """Launch form of the last step (GROUP_ONE_LAUNCH or GROUP_BRANCHES)."""
+        v = C.c_int()
+        _check(lib().sem_group_get_launch(self._h, C.byref(v)))
+        return v.value
 
     def close(self):
         if getattr(self, "_h", None):
