@@ -229,36 +229,11 @@ cudaError_t setup_o()
     return e;
 }
 
-using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiled encoder()
-{
-    static EncodeTiled fn = nullptr;
-    if (!fn) {
-        cudaDriverEntryPointQueryResult q;
-        void *p = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiled>(p);
-    }
-    return fn;
-}
-
 // 3-D map over the device layout (nxp, nz, planes) of float buffer `base` with box (bx, bz, 1);
 // planes = ny, or ny * nshot for levels that stack the shots along y.
 bool make_map(CUtensorMap &m, const float *base, const StencilTables &t, int bx, int bz, int64_t planes)
 {
-    EncodeTiled enc = encoder();
-    if (!enc) return false;
-    const cuuint64_t dims[3] = {(cuuint64_t)t.nxp, (cuuint64_t)t.nz, (cuuint64_t)planes};
-    const cuuint64_t strides[2] = {(cuuint64_t)t.nxp * 4, (cuuint64_t)t.nxp * t.nz * 4};
-    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)bz, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    return enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return encode_map_3d(m, base, t.nxp, t.nz, planes, bx, bz);
 }
 
 }  // namespace

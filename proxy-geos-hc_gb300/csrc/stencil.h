@@ -83,7 +83,7 @@ enum StencilMode { STENCIL_PLAIN = 0, STENCIL_RECORD_KP = 1, STENCIL_GRADIENT = 
 // One member of a group launch (k_group.cu): several boxes of orders 1..kGroupMaxOrder advanced
 // by one launch per step.  Lives in device memory; the launch's CTAs cta0.. belong to it.
 constexpr int kGroupMaxOrder = 4;
-struct alignas(64) GroupMember {
+struct GroupMember {  // 128-byte aligned, as its tensor maps
     StencilTables t;    // tensor maps of the member's levels, its tiling with the group's y-chunks
     StencilArgs a[2];   // [k]: pass arguments at group parity k (current level cur0 ^ k)
     SourceArgs src[2];  // [k]: source arguments at group parity k

@@ -659,6 +659,37 @@ __device__ __forceinline__ void stencil_cta(const CUtensorMap *rmap, const CUten
 }
 
 
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder()
+{
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+// Tensor map of a float buffer seen as (d0, d1, d2) row-major (d0 fastest) with box (b0, b1, 1).
+bool encode_map_3d(CUtensorMap &m, const float *base, int64_t d0, int64_t d1, int64_t d2, int b0, int b1)
+{
+    EncodeTiled enc = encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+    const cuuint64_t strides[2] = {(cuuint64_t)d0 * 4, (cuuint64_t)(d0 * d1) * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)b0, (cuuint32_t)b1, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Fill this translation unit's coefficient tables (orders 1..kMaxOrder).
 cudaError_t upload_stencil_constants()
 {
