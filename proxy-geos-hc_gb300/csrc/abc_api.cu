@@ -102,16 +102,14 @@ cudaError_t enqueue_correction(sem_abc *a)
         f.tiles = a->d_tiles;
         f.ntiles = a->ntiles;
         f.pos = a->d_pos;
-        f.p_new = x.p_new;
+        f.p_new = s->d_p[s->cur];
         f.p_cur = x.p_cur;
         f.hist = a->hist_now();
         f.hist_next = a->hist_next();
         f.sx = x.sx; f.sy = x.sy; f.sz = x.sz;
         f.nx = x.nx; f.nxp = x.nxp; f.ny = x.ny; f.nz = x.nz;
-        f.corr = a->d_corr;
-        cudaError_t e = abc_face(a->net->dev(), f, s->stream);
+        cudaError_t e = abc_face(a->net->dev(), f, s->stream);  // writes the new values in place
         if (e != cudaSuccess) return e;
-        if ((e = abc_apply(x, s->d_p[s->cur], nullptr, s->stream)) != cudaSuccess) return e;
         a->hcur ^= 1;
         return cudaSuccess;
     }

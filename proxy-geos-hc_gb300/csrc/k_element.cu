@@ -16,7 +16,8 @@
 // lane, one pencil per warp) for orders 1-4 and 16 for order 5 (36 pencils would exceed 1024
 // threads).  All lanes of a warp work on the same local pencil of different elements, so
 // coefficient indices are warp-uniform and shared-memory accesses are unit-stride.  Phases:
-//   A  the CTA's 32 connectivity rows (contiguous in HBM) -> shared, coalesced
+//   A  the connectivity rows of the tile two ahead (contiguous in HBM) -> shared by asynchronous
+//      copies (cp.async, no register staging), three row buffers in rotation
 //   B  gather p through the rows: each thread loads its x-pencil (registers + shared copy)
 //   C  x-direction contraction in registers
 //   D  z-direction (xi2) pencils from shared, result -> s_y
@@ -34,16 +35,37 @@ int coef_table_size(int order) { return 3 * (order + 1) * (order + 1); }
 
 namespace {
 
+// Elements per CTA at orders 1-4 (compile-time knob for sweeps: 32 = one element per lane and
+// one pencil per warp; 16 = two pencils per warp, half-size CTAs, twice as many per SM).
+#ifndef SEM_ELEMENT_TE
+#define SEM_ELEMENT_TE 32
+#endif
+
 template <int O, bool REF = false>
 struct ElemCfg {
     static constexpr int O1 = O + 1, NP = O1 * O1, NPE = O1 * O1 * O1;
-    static constexpr int TE = O <= 4 ? 32 : 16;  // elements per CTA
+    static constexpr int TE = O <= 4 ? SEM_ELEMENT_TE : 16;  // elements per CTA
     static constexpr int CS = NPE | 1;  // odd row stride: lanes hit distinct banks
     static constexpr int THREADS = TE * NP;
-    static constexpr int MINB = O == 1 ? 8 : O == 2 ? 5 : O == 3 ? 3 : O == 4 ? 2 : 2;
+    static constexpr int MINB = (O == 1 ? 8 : O == 2 ? 5 : O == 3 ? 3 : 2) * (O <= 4 ? 32 / SEM_ELEMENT_TE : 1);
     static constexpr int TAB = REF ? 3 * NPE * O1 : 3 * NP;  // coefficient floats in shared memory
-    static constexpr size_t SMEM = sizeof(int) * 2 * TE * CS + sizeof(float) * NPE * TE * 3 + sizeof(float) * TAB;
+    static constexpr int NBUF = 3;      // connectivity row buffers: this tile, the next two
+    static constexpr size_t SMEM = sizeof(int) * NBUF * TE * CS + sizeof(float) * NPE * TE * 3 + sizeof(float) * TAB;
 };
+
+// Asynchronous global -> shared copies (completion tracked per thread in commit groups).
+__device__ __forceinline__ uint32_t sh_addr(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sh_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sh_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until at most one group (the most recent) of this thread is still in flight
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // One direction of the element operator along one pencil: out = base * S p in difference form,
 // base = g_d * w_a * w_b of the pencil.
@@ -75,8 +97,8 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     using C = ElemCfg<O, REF>;
     constexpr int O1 = C::O1, NP = C::NP, NPE = C::NPE, CS = C::CS, TE = C::TE;
     extern __shared__ __align__(16) unsigned char smem[];
-    int *s_conn = reinterpret_cast<int *>(smem);  // [2][TE * CS]: this tile's rows and the next tile's
-    float *s_p = reinterpret_cast<float *>(s_conn + 2 * TE * CS);
+    int *s_conn = reinterpret_cast<int *>(smem);  // [NBUF][TE * CS]: this tile's rows and the next two tiles'
+    float *s_p = reinterpret_cast<float *>(s_conn + C::NBUF * TE * CS);
     float *s_y = s_p + NPE * TE;  // z-direction results
     float *s_w = s_y + NPE * TE;  // y-direction results
     float *s_tab = s_w + NPE * TE;
@@ -87,16 +109,30 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     int64_t t = blockIdx.x;
     if (t >= ntiles) return;
 
-    // connectivity rows of tile u (contiguous in HBM) into buffer b, coalesced
+    // connectivity rows of tile u (contiguous in HBM) into buffer b by asynchronous copies, then
+    // one commit group (also when u is past the end, so that every thread counts groups alike).
+    // Where the shared rows are unpadded (CS == NPE) and the array is 16-byte aligned (a caller's
+    // array need not be) the block is copied 16 bytes at a time: a tile's block then starts at a
+    // multiple of TE * NPE * 4 bytes, a multiple of 16, and so does its shared buffer.
     auto load_conn = [&](int64_t u, int b) {
-        const int64_t e0 = u * TE;
-        const int ne = (int)min((int64_t)TE, a.n_elem - e0);
-        const int32_t *cg = a.conn + e0 * NPE;
-        int *dst = s_conn + b * TE * CS;
-        for (int q = tid; q < ne * NPE; q += C::THREADS) {
-            const int e = q / NPE;
-            dst[e * CS + (q - e * NPE)] = __ldg(cg + q);
+        if (u < ntiles) {
+            const int64_t e0 = u * TE;
+            const int ne = (int)min((int64_t)TE, a.n_elem - e0);
+            const int32_t *cg = a.conn + e0 * NPE;
+            int *dst = s_conn + b * TE * CS;
+            int q0 = 0;
+            if constexpr (CS == NPE && (TE * NPE) % 4 == 0) {
+                if ((reinterpret_cast<uintptr_t>(a.conn) & 15) == 0) {
+                    q0 = ne * NPE / 4 * 4;
+                    for (int c = tid; c < q0 / 4; c += C::THREADS) cp_async16(dst + 4 * c, cg + 4 * c);
+                }
+            }
+            for (int q = q0 + tid; q < ne * NPE; q += C::THREADS) {
+                const int e = q / NPE;
+                cp_async4(dst + e * CS + (q - e * NPE), cg + q);
+            }
         }
+        cp_async_commit();
     };
     // the thread's x-pencil (local j, k fixed) of tile u through buffer b
     const int jx = warp % O1, kx = warp / O1;
@@ -110,30 +146,37 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
         }
     };
 
-    // A: coefficient table, the first tile's rows, and its pencil values
+    // A: coefficient table, the first two tiles' rows, and the first tile's pencil values
     for (int q = tid; q < C::TAB; q += C::THREADS) s_tab[q] = __ldg((REF ? a.rtab : a.tab) + q);
     load_conn(t, 0);
+    load_conn(t + gridDim.x, 1);
+    cp_async_wait_one();
     __syncthreads();
     float pn[O1];
     gather(t, 0, pn);
 
     // Persistent loop: while a tile runs its z- and y-directions and its scatter, the next
-    // tile's connectivity rows are in shared memory and its pencil values are in flight.
-    for (int b = 0; t < ntiles; t += gridDim.x, b ^= 1) {
+    // tile's connectivity rows are in shared memory and its pencil values are in flight, and the
+    // rows of the tile after it are being copied.  Buffer b holds this tile's rows, bn the
+    // next tile's, bf the one after (last used by the previous tile, whose final barrier has
+    // passed).
+    for (int b = 0; t < ntiles; t += gridDim.x, b = b == 2 ? 0 : b + 1) {
         const int64_t tn = t + gridDim.x;
+        const int bn = b == 2 ? 0 : b + 1, bf = bn == 2 ? 0 : bn + 1;
         const bool act = lane < (int)min((int64_t)TE, a.n_elem - t * TE);
-        // B: this tile's pencil values into shared memory; the next tile's rows into the other buffer
+        // B: this tile's pencil values into shared memory; copies of the rows two tiles ahead
         float px[O1];
 #pragma unroll
         for (int i = 0; i < O1; i++) {
             px[i] = pn[i];
             s_p[(i + O1 * jx + NP * kx) * TE + lane] = px[i];
         }
-        if (tn < ntiles) load_conn(tn, b ^ 1);
+        load_conn(tn + gridDim.x, bf);
         float yx[O1];
         if constexpr (REF) {
+            cp_async_wait_one();  // the next tile's rows (all but the copies just issued)
             __syncthreads();
-            if (tn < ntiles) gather(tn, b ^ 1, pn);
+            if (tn < ntiles) gather(tn, bn, pn);
             // C': K_e p at the thread's nodes as the reference forms it (SEMQkGLIntegrals.hpp:
             // 508-513): Y = sum over the row in increasing local index j of R[j] p[j], multiply and
             // add rounded separately.  The row's non-zero entries lie on the node's three lines;
@@ -161,8 +204,9 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
         } else {
             // C: x-direction in registers
             pencil_apply<O>(a, px, s_tab[0 * NP + jx + O1 * kx], yx);
+            cp_async_wait_one();  // the next tile's rows (all but the copies just issued)
             __syncthreads();
-            if (tn < ntiles) gather(tn, b ^ 1, pn);
+            if (tn < ntiles) gather(tn, bn, pn);
             // D: z-direction (local index j varies) into s_y, and E: y-direction (local index k
             // varies) into s_w; both only read s_p, so no barrier between them
             {

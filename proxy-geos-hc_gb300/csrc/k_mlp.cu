@@ -238,8 +238,8 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
             for (int j = 0; j < 4; j++) acc[mt][nt][j] = 0.f;
 #pragma unroll
     for (int ks = 0; ks < kMlpInPad / 16; ks++) {
-        const int k0 = ks * 16 + q * 2;
         uint32_t a[2][4];
+        const int k0 = ks * 16 + q * 2;
 #pragma unroll
         for (int mt = 0; mt < 2; mt++) {
             const int r = wr + mt * 16 + g;
@@ -251,9 +251,8 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
             const int n = nt * 8 + g;
-            uint32_t b[2];
-            b[0] = *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0);
-            b[1] = *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0 + 8);
+            const uint32_t b[2] = {*reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0),
+                                   *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0 + 8)};
             mma16816(acc[0][nt], a[0], b);
             mma16816(acc[1][nt], a[1], b);
         }
@@ -282,9 +281,8 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
             const int n = nt * 8 + g;
-            uint32_t b[2];
-            b[0] = *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0);
-            b[1] = *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0 + 8);
+            const uint32_t b[2] = {*reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0),
+                                   *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0 + 8)};
             mma16816(acc[0][nt], h[0][ks], b);
             mma16816(acc[1][nt], h[1][ks], b);
         }
@@ -585,7 +583,7 @@ __global__ void __launch_bounds__(128, 4) k_abc_correction(const MlpDev net, con
                         const float x = (okx[dx] && oky[dy] && okz[dz])
                                             ? lv[(ix + dx - 1) + (iz + dz - 1) * a.nxp + (iy + dy - 1) * plane]
                                             : 0.f;
-                        v[nb] = l == 1 ? x * ((fx[dx] * fy[dy]) * fz[dz]) : x;
+                        v[nb] = l == 1 ? x * ((fx[dx] * fz[dz]) * fy[dy]) : x;
                     }
                 };
                 float v[3][27];
@@ -675,21 +673,23 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
             auto along = [&](int axis) { return axis == 0 ? dx : (axis == 1 ? dy : dz); };
             offs[threadIdx.x] = along(f.axis_n) * f.inward * kPD + along(f.axis_v) * kPU + along(f.axis_u);
         }
-        // stage the face and inside planes of the three levels with a one-node rim; x-faces step
-        // through the depth fastest (adjacent in memory), the others along u (rows along x).  All
-        // of a thread's loads are issued first (one round trip), then stored.
+        // stage the face and inside planes of the three levels with a one-node rim: a thread takes
+        // a position (depth, v, u) and loads it from all three levels, sharing the index
+        // arithmetic and the node's sponge factor.  x-faces step through the depth fastest
+        // (adjacent in memory), the others along u (rows along x).  All of a thread's loads are
+        // issued first (one round trip), then stored.
         const bool depth_fast = f.axis_n == 0;
-        constexpr int NSTAGE = 3 * 2 * kPD, KS = (NSTAGE + T - 1) / T;
-        // element i of the patch: level, depth (1: face, 2: inside), position along v and u
-        auto decode = [&](int i, int &l, int &di, int &vv, int &uu) {
+        constexpr int NPOS = 2 * kPD, KS = (NPOS + T - 1) / T;
+        // position i of the patch: depth (1: face, 2: inside), position along v and u
+        auto decode = [&](int i, int &di, int &vv, int &uu) {
             if (depth_fast) {
                 di = i % 2 + 1;
                 const int r = i / 2;
-                uu = r % kPU; vv = (r / kPU) % kPV; l = r / kPD;
+                uu = r % kPU; vv = r / kPU;
             } else {
                 uu = i % kPU;
                 const int r = i / kPU;
-                vv = r % kPV; di = (r / kPV) % 2 + 1; l = r / (2 * kPV);
+                vv = r % kPV; di = r / kPV + 1;
             }
         };
         // node coordinates by axis (selects, not an indexed array: they stay in registers)
@@ -699,41 +699,52 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
             cy = f.axis_u == 1 ? cu : (f.axis_v == 1 ? cv : cn);
             cz = f.axis_u == 2 ? cu : (f.axis_v == 2 ? cv : cn);
         };
-        float sval[KS], sfac[KS];
+        // p^{n+1} of a boundary node is the stored p^{n-1} twice damped (the step keeps the
+        // Dirichlet value): s * (s * p^{n-1}) = s * hist, the same bits, so boundary nodes take
+        // level 0 from the history and this kernel can write their new values in place (no tile
+        // reads p^{n+1} of a boundary node).  s = (sx*sz)*sy, as the step rounds it.
+        float v0s[KS], v1s[KS], v2s[KS], sfs[KS];
+        bool bnds[KS];
 #pragma unroll
         for (int k = 0; k < KS; k++) {
             const int i = threadIdx.x + k * T;
-            sval[k] = 0.f;
-            sfac[k] = 1.f;
-            if (i < NSTAGE) {
-                int l, di, vv, uu, cx, cy, cz;
-                decode(i, l, di, vv, uu);
+            v0s[k] = v1s[k] = v2s[k] = 0.f;
+            sfs[k] = 1.f;
+            bnds[k] = false;
+            if (i < NPOS) {
+                int di, vv, uu, cx, cy, cz;
+                decode(i, di, vv, uu);
                 coords(di, vv, uu, cx, cy, cz);
                 if (cx >= 0 && cx < a.nx && cy >= 0 && cy < a.ny && cz >= 0 && cz < a.nz) {
                     const int64_t qn = cx + (int64_t)cz * a.nxp + (int64_t)cy * plane;
-                    sval[k] = (l == 0 ? a.p_new : (l == 1 ? a.p_cur : a.hist))[qn];
-                    if (l == 1 && a.sx) sfac[k] = (__ldg(a.sx + cx) * __ldg(a.sy + cy)) * __ldg(a.sz + cz);
+                    bnds[k] = cx == 0 || cx == a.nx - 1 || cy == 0 || cy == a.ny - 1 || cz == 0 || cz == a.nz - 1;
+                    v2s[k] = a.hist[qn];
+                    v1s[k] = a.p_cur[qn];
+                    if (!bnds[k]) v0s[k] = a.p_new[qn];
+                    if (a.sx) sfs[k] = (__ldg(a.sx + cx) * __ldg(a.sz + cz)) * __ldg(a.sy + cy);
                 }
             }
         }
 #pragma unroll
         for (int k = 0; k < KS; k++) {
             const int i = threadIdx.x + k * T;
-            if (i < NSTAGE) {
-                int l, di, vv, uu, cx, cy, cz;
-                decode(i, l, di, vv, uu);
-                float val = sval[k];
-                if (l == 1) {
-                    val = val * sfac[k];  // p^n is stored without its last sponge factor
-                    // p^n of the tile's own nodes and their inside neighbours: the next step's
-                    // p^{n-1} (every node of the two-node shell is one of these for some tile)
-                    const int us = u0 - 1 + uu, vs = v0 - 1 + vv;
-                    if (uu >= 1 && uu <= kFaceTU && vv >= 1 && vv <= kFaceTV && us < f.uhi && vs < f.vhi) {
-                        coords(di, vv, uu, cx, cy, cz);
-                        a.hist_next[cx + (int64_t)cz * a.nxp + (int64_t)cy * plane] = val;
-                    }
+            if (i < NPOS) {
+                int di, vv, uu;
+                decode(i, di, vv, uu);
+                const float p0 = bnds[k] ? v2s[k] * sfs[k] : v0s[k];
+                const float p1 = v1s[k] * sfs[k];  // p^n is stored without its last sponge factor
+                // p^n of the tile's own nodes and their inside neighbours: the next step's
+                // p^{n-1} (every node of the two-node shell is one of these for some tile)
+                const int us = u0 - 1 + uu, vs = v0 - 1 + vv;
+                if (uu >= 1 && uu <= kFaceTU && vv >= 1 && vv <= kFaceTV && us < f.uhi && vs < f.vhi) {
+                    int cx, cy, cz;
+                    coords(di, vv, uu, cx, cy, cz);
+                    a.hist_next[cx + (int64_t)cz * a.nxp + (int64_t)cy * plane] = p1;
                 }
-                patch[l * kPL + di * kPD + vv * kPU + uu] = val;
+                const int o = di * kPD + vv * kPU + uu;
+                patch[o] = p0;
+                patch[kPL + o] = p1;
+                patch[2 * kPL + o] = v2s[k];
             }
         }
         __syncthreads();
@@ -784,11 +795,11 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
 #pragma unroll
                 for (int hrow = 0; hrow < 2; hrow++) {
                     const int rr = w * 32 + mt * 16 + g + hrow * 8;
-                    const int64_t pr = a.pos[t * T + rr];
-                    if (pr >= 0) {
-                        const float vnew = scale[rr] * fminf(fmaxf(yv[mt][hrow], -1.f), 1.f);
-                        const int b = kPD + (rr / kFaceTU + 1) * kPU + (rr % kFaceTU + 1);
-                        a.corr[pr] = vnew - patch[b];  // minus p^{n+1} of the node (level 0)
+                    if (a.pos[t * T + rr] >= 0) {
+                        int cx, cy, cz;
+                        coords(1, rr / kFaceTU + 1, rr % kFaceTU + 1, cx, cy, cz);
+                        a.p_new[cx + (int64_t)cz * a.nxp + (int64_t)cy * plane] =
+                            scale[rr] * fminf(fmaxf(yv[mt][hrow], -1.f), 1.f);
                     }
                 }
     }
@@ -808,7 +819,7 @@ __global__ void k_abc_history(const int64_t *shell, int64_t n, const float *p_cu
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t q0 = shell[i];
         const int64_t iy = q0 / plane, rr = q0 - iy * plane, iz = rr / nxp, ix = rr - iz * nxp;
-        hist[q0] = p_cur[q0] * (sx ? (sx[ix] * sy[iy]) * sz[iz] : 1.f);
+        hist[q0] = p_cur[q0] * (sx ? (sx[ix] * sz[iz]) * sy[iy] : 1.f);
     }
 }
 

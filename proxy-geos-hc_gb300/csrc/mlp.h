@@ -59,16 +59,16 @@ struct AbcFaceArgs {
     const int4 *tiles;     // (face, u0, v0, 0) per tile
     int64_t ntiles;
     const int64_t *pos;    // [ntiles * kMlpTile]: position of each tile row in the strip (-1: none)
-    const float *p_new;    // p^{n+1} (sponge applied)
+    float *p_new;          // p^{n+1} (sponge applied); out: the boundary nodes' new values
     const float *p_cur;    // p^n stored without its last sponge factor
     const float *hist;     // p^{n-1} (actual values) on the two-node shell, device layout
     float *hist_next;      // out: p^n (actual values) on the two-node shell, device layout
     const float *sx, *sy, *sz;  // sponge factors (null: none)
     int64_t nx, nxp, ny, nz;
-    float *corr;           // out: new value minus p^{n+1}, per strip position
 };
-// Face-tiled correction (the features, network, output and clipping of abc_correction with
-// absolute values), and p^n into hist_next on the shell.
+// Face-tiled boundary values (the features, network, output and clipping of abc_correction with
+// absolute values) written into p_new, and p^n into hist_next on the shell.  p^{n+1} of the
+// boundary nodes is taken as s * hist (what the step leaves there), the rest from p_new.
 cudaError_t abc_face(const MlpDev &net, const AbcFaceArgs &a, cudaStream_t s);
 
 // bf16 conversion of the FP32 master weights into the device layout.
