@@ -25,6 +25,8 @@ using namespace semgb;
 struct sem_mlp {
     float *d_master = nullptr;  // FP32 parameters (mlp.h layout)
     float *d_m = nullptr, *d_v = nullptr, *d_grad = nullptr;
+    float *d_part = nullptr;       // per-CTA partial gradients [kMlpMaxCTAs][kMlpParams]
+    double *d_part_loss = nullptr;  // per-CTA partial losses [kMlpMaxCTAs]
     uint16_t *d_w1 = nullptr, *d_w2 = nullptr;
     float *d_b1 = nullptr, *d_b2 = nullptr, *d_w3 = nullptr, *d_b3 = nullptr;
     double *d_loss = nullptr;
@@ -132,6 +134,7 @@ int sem_mlp_destroy(sem_mlp *m)
     if (!m) return SEM_OK;
     if (m->stream) cudaStreamSynchronize(m->stream);
     dfree(m->d_master); dfree(m->d_m); dfree(m->d_v); dfree(m->d_grad);
+    dfree(m->d_part); dfree(m->d_part_loss);
     dfree(m->d_w1); dfree(m->d_w2); dfree(m->d_b1); dfree(m->d_b2); dfree(m->d_w3); dfree(m->d_b3);
     dfree(m->d_loss);
     if (m->stream) cudaStreamDestroy(m->stream);
@@ -150,6 +153,8 @@ int sem_mlp_create(uint64_t seed, sem_mlp **out)
     if (e == cudaSuccess) e = dalloc(&m->d_m, kMlpParams);
     if (e == cudaSuccess) e = dalloc(&m->d_v, kMlpParams);
     if (e == cudaSuccess) e = dalloc(&m->d_grad, kMlpParams);
+    if (e == cudaSuccess) e = dalloc(&m->d_part, (size_t)kMlpMaxCTAs * kMlpParams);
+    if (e == cudaSuccess) e = dalloc(&m->d_part_loss, (size_t)kMlpMaxCTAs);
     if (e == cudaSuccess) e = dalloc(&m->d_w1, kMlpHidden * kMlpInPad);
     if (e == cudaSuccess) e = dalloc(&m->d_w2, kMlpHidden * kMlpHidden);
     if (e == cudaSuccess) e = dalloc(&m->d_b1, kMlpHidden);
@@ -234,7 +239,7 @@ int sem_mlp_loss_grad(sem_mlp *m, int64_t n, const float *x, const float *t, dou
     if (e == cudaSuccess) e = cudaMemcpy(dt, t, (size_t)n * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->d_grad, 0, kMlpParams * 4, m->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->d_loss, 0, 8, m->stream);
-    if (e == cudaSuccess) e = mlp_loss_grad(m->dev(), dx, dt, n, m->d_loss, m->d_grad, m->stream);
+    if (e == cudaSuccess) e = mlp_loss_grad(m->dev(), dx, dt, n, m->d_loss, m->d_grad, m->d_part, m->d_part_loss, m->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
     if (e == cudaSuccess && loss) e = cudaMemcpy(loss, m->d_loss, 8, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && grad) e = cudaMemcpy(grad, m->d_grad, kMlpParams * 4, cudaMemcpyDeviceToHost);
@@ -274,7 +279,7 @@ int sem_mlp_train(sem_mlp *m, int64_t n, const float *x, const float *t, int epo
             e = mlp_gather_rows(dx, dt, dperm + b0, nb, bx, bt, m->stream);
             if (e == cudaSuccess) e = cudaMemsetAsync(m->d_grad, 0, kMlpParams * 4, m->stream);
             if (e == cudaSuccess) e = cudaMemsetAsync(m->d_loss, 0, 8, m->stream);
-            if (e == cudaSuccess) e = mlp_loss_grad(m->dev(), bx, bt, nb, m->d_loss, m->d_grad, m->stream);
+            if (e == cudaSuccess) e = mlp_loss_grad(m->dev(), bx, bt, nb, m->d_loss, m->d_grad, m->d_part, m->d_part_loss, m->stream);
             if (e == cudaSuccess) e = mlp_adam(m->d_master, m->d_grad, m->d_m, m->d_v, ++m->adam_t, lr, m->stream);
             if (e == cudaSuccess)
                 e = mlp_pack(m->d_master, m->d_w1, m->d_w2, m->d_b1, m->d_b2, m->d_w3, m->d_b3, m->stream);

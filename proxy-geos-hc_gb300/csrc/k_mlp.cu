@@ -354,7 +354,7 @@ struct TrainSmem {
 };
 
 __global__ void __launch_bounds__(128) k_mlp_train_pass(const MlpDev net, const float *x, const float *t, int64_t n,
-                                                        double *loss, float *grad)
+                                                        double *part_loss, float *part)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
@@ -448,19 +448,40 @@ __global__ void __launch_bounds__(128) k_mlp_train_pass(const MlpDev net, const 
         __syncthreads();
     }
     __syncthreads();
+    // this CTA's partial sums (the W3 range is written by k_mlp_grad_w3)
+    float *pg = part + (int64_t)blockIdx.x * kMlpParams;
     for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x)
-        if (ts.g[i] != 0.f) atomicAdd(grad + i, ts.g[i]);
-    // loss: quad leaders hold partial sums
+        if (i < kOffW3 || i >= kOffW3 + H) pg[i] = ts.g[i];
+    // loss: quad leaders hold partial sums; warps added in order
     lsum += __shfl_xor_sync(0xffffffffu, lsum, 4);
     lsum += __shfl_xor_sync(0xffffffffu, lsum, 8);
     lsum += __shfl_xor_sync(0xffffffffu, lsum, 16);
-    if (lane == 0) atomicAdd(loss, lsum / (double)n);
+    __shared__ double wl[4];
+    if (lane == 0) wl[w] = lsum;
+    __syncthreads();
+    if (threadIdx.x == 0) part_loss[blockIdx.x] = (((wl[0] + wl[1]) + wl[2]) + wl[3]) / (double)n;
+}
+
+// grad[i] += sum over CTAs b (in order) of part[b][i]; *loss += sum of part_loss[b] in order
+__global__ void k_mlp_reduce(const float *part, const double *part_loss, int nb, float *grad, double *loss)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kMlpParams) {
+        float a = 0.f;
+        for (int b = 0; b < nb; b++) a += part[(int64_t)b * kMlpParams + i];
+        grad[i] += a;
+    }
+    if (i == 0) {
+        double l = 0.0;
+        for (int b = 0; b < nb; b++) l += part_loss[b];
+        *loss += l;
+    }
 }
 
 // dw3[c] = sum_r dy[r] GELU(z2[r][c]) needs the forward activations the training pass
 // overwrites; this pass recomputes them (forward only) and accumulates dw3.
 __global__ void __launch_bounds__(128) k_mlp_grad_w3(const MlpDev net, const float *x, const float *t, int64_t n,
-                                                     float *grad)
+                                                     float *part)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
@@ -497,7 +518,7 @@ __global__ void __launch_bounds__(128) k_mlp_grad_w3(const MlpDev net, const flo
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < H; i += blockDim.x) atomicAdd(grad + kOffW3 + i, gw3[i]);
+    for (int i = threadIdx.x; i < H; i += blockDim.x) part[(int64_t)blockIdx.x * kMlpParams + kOffW3 + i] = gw3[i];
 }
 
 __global__ void k_mlp_pack(const float *m, uint16_t *w1, uint16_t *w2, float *b1, float *b2, float *w3, float *b3)
@@ -866,18 +887,22 @@ cudaError_t mlp_forward(const MlpDev &net, const float *x, float *y, int64_t n, 
 }
 
 cudaError_t mlp_loss_grad(const MlpDev &net, const float *x, const float *t, int64_t n, double *loss, float *grad,
-                          cudaStream_t s)
+                          float *part, double *part_loss, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    const int nb = grid_for(n);
+    static_assert(kMlpMaxCTAs >= 152 * 4, "partial-sum rows for every CTA of grid_for");
     size_t sm = smem_train();
     cudaError_t e = cudaFuncSetAttribute(k_mlp_train_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_mlp_train_pass<<<grid_for(n), T, sm, s>>>(net, x, t, n, loss, grad);
+    k_mlp_train_pass<<<nb, T, sm, s>>>(net, x, t, n, part_loss, part);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     sm = smem_w3();
     if ((e = cudaFuncSetAttribute(k_mlp_grad_w3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
         return e;
-    k_mlp_grad_w3<<<grid_for(n), T, sm, s>>>(net, x, t, n, grad);
+    k_mlp_grad_w3<<<nb, T, sm, s>>>(net, x, t, n, part);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_mlp_reduce<<<(kMlpParams + 255) / 256, 256, 0, s>>>(part, part_loss, nb, grad, loss);
     return cudaGetLastError();
 }
 

@@ -78,8 +78,11 @@ cudaError_t mlp_pack(const float *master, uint16_t *w1, uint16_t *w2, float *b1,
 cudaError_t mlp_forward(const MlpDev &net, const float *x, float *y, int64_t n, cudaStream_t s);
 // Loss 1/n sum (net(x_i) - t_i)^2 accumulated into *loss (double), gradients with respect to the
 // master parameters accumulated into grad (FP32 [kMlpParams]).
+// Deterministic: every CTA writes its partial sums to part ([kMlpMaxCTAs][kMlpParams]) and
+// part_loss ([kMlpMaxCTAs]), and one pass adds them in CTA order.
+constexpr int kMlpMaxCTAs = 152 * 4;
 cudaError_t mlp_loss_grad(const MlpDev &net, const float *x, const float *t, int64_t n, double *loss, float *grad,
-                          cudaStream_t s);
+                          float *part, double *part_loss, cudaStream_t s);
 // bx[i] = x[idx[i]], bt[i] = t[idx[i]] for i < nb (minibatch rows).
 cudaError_t mlp_gather_rows(const float *x, const float *t, const int64_t *idx, int64_t nb, float *bx, float *bt,
                             cudaStream_t s);

@@ -61,6 +61,25 @@ def test_training_reduces_loss(semgb_lib, cuda_device):
     assert l1 < 0.05 * l0, (l0, l1, losses)
 
 
+def test_training_is_reproducible(semgb_lib, cuda_device):
+    """Per-CTA partial gradients are added in CTA order (no atomics): the same seed and data give
+    the same parameters and losses bit for bit, so the boundary's training is repeatable."""
+    semgb = semgb_lib
+    rng = np.random.default_rng(18)
+    x = rng.uniform(-1, 1, (9000, 81)).astype(np.float32)
+    t = (np.tanh(x[:, :27].sum(1) * 0.3) - 0.2 * x[:, 40]).astype(np.float32)
+    runs = []
+    for _ in range(2):
+        net = semgb.Mlp(17)
+        losses = net.train(x, t, epochs=3, batch=1000, lr=2e-3, seed=5)
+        g = net.loss_grad(x, t)
+        runs.append((net.params, losses, g[0], g[1]))
+        net.close()
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
+    assert runs[0][2] == runs[1][2] and np.array_equal(runs[0][3], runs[1][3])
+
+
 def _solver(semgb, wl):
     mesh, s = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
     return mesh, s
@@ -112,9 +131,9 @@ def test_trained_network_reduces_reflections(semgb_lib, cuda_device):
     """Thin sponge (3 elements) with and without the trained network on the boundary nodes,
     against a padded run: the network (best of its training rounds) lowers the reflected energy
     in the interior, for the training source and for a source position not used in training.
-    Training is not bit-reproducible (gradients are summed with atomics) and the rounds are
-    selected on the training source; measured ratios are 0.35-0.45 for it (bound 0.6) and
-    0.28-0.60 for the held-out source (bound 0.75)."""
+    Training is bit-reproducible (per-CTA gradient sums added in order), so the ratios are fixed:
+    measured 0.590 for the training source (bound 0.6) and 0.394 for the held-out source (bound
+    0.75)."""
     semgb = semgb_lib
     from semgb import learned_boundary as LB
     from semgb import workloads as W
