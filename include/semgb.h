@@ -422,6 +422,8 @@ int sem_mlp_loss_grad(sem_mlp *net, int64_t n, const float *x, const float *t, d
  * samples (shuffled with `seed`); losses[epoch] = mean minibatch loss (may be NULL). */
 int sem_mlp_train(sem_mlp *net, int64_t n, const float *x, const float *t, int epochs, int batch, float lr,
                   uint64_t seed, double *losses);
+/* One Adam step of the network's parameters with a given gradient (host, parameter count). */
+int sem_mlp_adam_step(sem_mlp *net, const float *grad, float lr);
 
 /* Attach `net` to a solver (stencil pass) for the strip of `layer_elems` elements. */
 int sem_abc_create(sem_solver *s, sem_mlp *net, int layer_elems, sem_abc **out);
@@ -439,6 +441,17 @@ int sem_abc_set_history(sem_abc *a, const float *p_prev);
 /* The network inputs of every strip node for the step that just ran: x [n_nodes][81] already
  * divided by scale [n_nodes] (may be NULL), as the correction kernel forms them. */
 int sem_abc_features(sem_abc *a, float *x, float *scale);
+/* Training through the adjoint of the whole time loop (network on the boundary nodes, layer 0).
+ * Runs n_steps corrected steps from rest (the solver and the history are reset first) and
+ * returns loss = sum over steps m = 1..n_steps and region nodes r of (p^m_r - ref[m-1][r])^2
+ * (roi_nodes: reference numbering; ref: host [n_steps][n_roi]).  With grad non-NULL (host,
+ * the network's parameter count) the gradient of the loss with respect to the network's
+ * parameters is computed by the adjoint of every step, newest first: the network's own backward
+ * kernels at the boundary nodes (through the division by the neighbourhood's largest magnitude
+ * and the clipping) and the adjoint leapfrog of the stencil pass, from the recorded levels.
+ * Sources must lie at least two nodes inside the box.  The solver is left after the n_steps. */
+int sem_abc_bptt(sem_abc *a, int n_steps, int n_roi, const int64_t *roi_nodes, const float *ref, double *loss,
+                 float *grad);
 
 /* ------------------------------------------------------------------------------------------
  * Output formats.  One container for traces and snapshots: 8-byte magic, little-endian uint64

@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "semgb", "_lib")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsemgb.so")
 
-SOURCES = ["api.cu", "adjoint_api.cu", "batch_api.cu", "group_api.cu", "k_group.cu", "abc_api.cu", "k_mlp.cu", "k_element.cu", "k_update.cu", "k_stencil.cu", "k_batch.cu", "noalloc.cu",
+SOURCES = ["api.cu", "adjoint_api.cu", "batch_api.cu", "group_api.cu", "k_group.cu", "k_bptt.cu", "abc_api.cu", "k_mlp.cu", "k_element.cu", "k_update.cu", "k_stencil.cu", "k_batch.cu", "noalloc.cu",
            "host_util.cpp", "formats.cpp"]
 HEADERS = ["abi.h", "stencil_body.cuh", "solver.h", "batch.h", "mlp.h", "kernels.h", "stencil.h", "host_util.h", "tma.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -298,6 +298,18 @@ int sem_mlp_train(sem_mlp *m, int64_t n, const float *x, const float *t, int epo
     GUARD_END
 }
 
+int sem_mlp_adam_step(sem_mlp *m, const float *grad, float lr)
+{
+    GUARD_BEGIN
+    if (!m || !grad || !(lr > 0)) return sem_fail(SEM_ERR_ARG, "bad arguments");
+    CUDA_TRY(cudaMemcpyAsync(m->d_grad, grad, kMlpParams * 4, cudaMemcpyHostToDevice, m->stream));
+    CUDA_TRY(mlp_adam(m->d_master, m->d_grad, m->d_m, m->d_v, ++m->adam_t, lr, m->stream));
+    CUDA_TRY(mlp_pack(m->d_master, m->d_w1, m->d_w2, m->d_b1, m->d_b2, m->d_w3, m->d_b3, m->stream));
+    CUDA_TRY(cudaStreamSynchronize(m->stream));
+    return SEM_OK;
+    GUARD_END
+}
+
 // ---- boundary ------------------------------------------------------------------------------
 
 int sem_abc_destroy(sem_abc *a)
@@ -490,6 +502,146 @@ int sem_abc_step(sem_abc *a, int n_steps)
         CUDA_TRY(enqueue_correction(a));
     }
     s->steps_done += n_steps;
+    return SEM_OK;
+    GUARD_END
+}
+
+int sem_abc_bptt(sem_abc *a, int n_steps, int n_roi, const int64_t *roi_nodes, const float *ref, double *loss,
+                 float *grad)
+{
+    GUARD_BEGIN
+    if (!a || n_steps < 1 || n_roi < 0 || (n_roi > 0 && (!roi_nodes || !ref)) || !loss)
+        return sem_fail(SEM_ERR_ARG, "bad arguments");
+    if (!a->face) return sem_fail(SEM_ERR_STATE, "the adjoint runs with the network on the boundary nodes (layer 0)");
+    sem_solver *s = a->s;
+    const Box &b = s->mesh->box;
+    // sources must lie outside every boundary node's neighbourhood: the recorded levels do not
+    // hold the source term a step adds before it reads them
+    for (int64_t q : s->src_node) {
+        const int64_t iy = q / (b.nxp * b.nz), r = q - iy * b.nxp * b.nz, iz = r / b.nxp, ix = r - iz * b.nxp;
+        if (ix < 2 || ix > b.nx - 3 || iy < 2 || iy > b.ny - 3 || iz < 2 || iz > b.nz - 3)
+            return sem_fail(SEM_ERR_ARG, "a source lies within two nodes of the boundary");
+    }
+    std::vector<int64_t> roi(n_roi);
+    for (int r = 0; r < n_roi; r++) {
+        if (roi_nodes[r] < 0 || roi_nodes[r] >= b.n_nodes) return sem_fail(SEM_ERR_ARG, "region node out of range");
+        roi[r] = to_internal(b, roi_nodes[r]);
+    }
+    int rc = sem_solver_reset(s);
+    if (rc) return rc;
+    if ((rc = sem_abc_reset(a))) return rc;
+    if ((rc = solver_prepare(s, n_steps))) return rc;
+    const int64_t n_int = b.n_int, nb = a->n;
+    cudaStream_t st = s->stream;
+
+    // work arrays (freed on every exit path)
+    float *rec = nullptr, *x = nullptr, *dx = nullptr, *scale = nullptr, *y = nullptr, *g = nullptr, *dy = nullptr;
+    float *A[3] = {nullptr, nullptr, nullptr}, *v = nullptr, *dref = nullptr;
+    int *kstar = nullptr, *sidx = nullptr;
+    int64_t *droi = nullptr;
+    double *dloss = nullptr, *dnull = nullptr;
+    auto release = [&]() {
+        cudaStreamSynchronize(st);
+        dfree(rec); dfree(x); dfree(dx); dfree(scale); dfree(y); dfree(g); dfree(dy);
+        for (auto &p : A) dfree(p);
+        dfree(v); dfree(dref); dfree(kstar); dfree(sidx); dfree(droi); dfree(dloss); dfree(dnull);
+    };
+    cudaError_t e = dalloc(&rec, (size_t)(n_steps + 2) * n_int);
+    if (e == cudaSuccess) e = dalloc(&x, (size_t)nb * kMlpIn);
+    if (e == cudaSuccess) e = dalloc(&dx, (size_t)nb * kMlpIn);
+    if (e == cudaSuccess) e = dalloc(&scale, (size_t)nb);
+    if (e == cudaSuccess) e = dalloc(&y, (size_t)nb);
+    if (e == cudaSuccess) e = dalloc(&g, (size_t)nb);
+    if (e == cudaSuccess) e = dalloc(&dy, (size_t)nb);
+    for (auto &p : A)
+        if (e == cudaSuccess) e = dalloc(&p, (size_t)n_int);
+    if (e == cudaSuccess) e = dalloc(&v, (size_t)n_int);
+    if (e == cudaSuccess && n_roi > 0) e = dalloc(&dref, (size_t)n_steps * n_roi);
+    if (e == cudaSuccess) e = dalloc(&kstar, (size_t)nb);
+    if (e == cudaSuccess) e = dalloc(&sidx, (size_t)n_int);
+    if (e == cudaSuccess && n_roi > 0) e = dalloc(&droi, (size_t)n_roi);
+    if (e == cudaSuccess) e = dalloc(&dloss, 1);
+    if (e == cudaSuccess) e = dalloc(&dnull, 1);
+    if (e == cudaSuccess) {
+        std::vector<int64_t> nodes(nb);
+        e = cudaMemcpy(nodes.data(), a->d_nodes, nb * 8, cudaMemcpyDeviceToHost);
+        std::vector<int> map(n_int, -1);
+        for (int64_t i = 0; i < nb; i++) map[nodes[i]] = (int)i;
+        if (e == cudaSuccess) e = cudaMemcpy(sidx, map.data(), n_int * 4, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess && n_roi > 0) e = cudaMemcpy(droi, roi.data(), n_roi * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n_roi > 0)
+        e = cudaMemcpy(dref, ref, (size_t)n_steps * n_roi * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dloss, 0, 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(rec, 0, 2 * n_int * 4, st);  // p^{-1} = p^0 = 0: from rest
+    // forward, the levels after every step recorded
+    for (int m = 1; m <= n_steps && e == cudaSuccess; m++) {
+        e = solver_enqueue_step(s, s->cur);
+        s->cur ^= 1;
+        if (e == cudaSuccess) e = enqueue_correction(a);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(rec + (size_t)(m + 1) * n_int, s->d_p[s->cur], n_int * 4, cudaMemcpyDeviceToDevice, st);
+    }
+    s->steps_done += n_steps;
+    BpttFields f{};
+    f.nx = (int)b.nx; f.ny = (int)b.ny; f.nz = (int)b.nz;
+    f.nxp = b.nxp; f.n_int = n_int;
+    f.sx = s->sponge ? s->d_sx : nullptr;
+    f.sy = s->sponge ? s->d_sy : nullptr;
+    f.sz = s->sponge ? s->d_sz : nullptr;
+    f.nodes = a->d_nodes; f.nb = nb; f.sidx = sidx;
+    f.x = x; f.scale = scale; f.kstar = kstar; f.y = y; f.g = g; f.dy = dy; f.dx = dx;
+    for (int k = 0; k < 3; k++) f.a[k] = A[k];
+    f.v = v; f.roi = droi; f.n_roi = n_roi;
+    for (auto p : A)
+        if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, n_int * 4, st);
+    if (!grad) {
+        // the loss only
+        for (int m = 1; m <= n_steps && e == cudaSuccess; m++)
+            e = bptt_loss(f, rec + (size_t)(m + 1) * n_int, dref + (size_t)(m - 1) * n_roi, dloss, st);
+    } else {
+        BpttOperator op{};
+        op.order = b.order;
+        Gll gl;
+        gll_tables(b.order, gl);
+        stencil_table(gl, op.T);
+        const int W = 2 * b.order + 1;
+        for (int l = 0; l < b.order; l++) {
+            // the direct form's diagonal: minus the rounded row sum, as the stencil pass uses it
+            double sum = 0;
+            for (int d = -b.order; d <= b.order; d++)
+                if (d != 0) sum += op.T[l * W + d + b.order];
+            op.T[l * W + b.order] = (float)-sum;
+            op.wa[l] = s->stencil->wa[l];
+        }
+        for (int k = 0; k < 3; k++) op.g[k] = s->stencil->g[k];
+        sem_mlp *net = a->net;
+        if (e == cudaSuccess) e = cudaMemsetAsync(net->d_grad, 0, kMlpParams * 4, st);
+        for (int m = n_steps; m >= 1 && e == cudaSuccess; m--) {
+            const float *lm = rec + (size_t)(m + 1) * n_int, *lm1 = rec + (size_t)m * n_int,
+                        *lm2 = rec + (size_t)(m - 1) * n_int;
+            e = bptt_loss(f, lm, dref + (size_t)(m - 1) * n_roi, dloss, st);
+            if (e == cudaSuccess) e = bptt_features(f, lm, lm1, lm2, st);
+            if (e == cudaSuccess) e = mlp_forward(net->dev(), x, y, nb, st);
+            if (e == cudaSuccess) e = bptt_dy(f, st);
+            if (e == cudaSuccess)
+                e = mlp_loss_grad(net->dev(), x, nullptr, nb, dnull, net->d_grad, net->d_part, net->d_part_loss, st,
+                                  dy, dx);
+            if (e == cudaSuccess) e = bptt_scatter(f, st);
+            if (e == cudaSuccess) e = bptt_interior(f, op, s->d_a, st);
+            // the adjoints move one level back: out^{m-1} becomes the newest
+            float *old = f.a[0];
+            f.a[0] = f.a[1];
+            f.a[1] = f.a[2];
+            f.a[2] = old;
+            if (e == cudaSuccess) e = cudaMemsetAsync(old, 0, n_int * 4, st);
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(grad, net->d_grad, kMlpParams * 4, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(loss, dloss, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    release();
+    CUDA_TRY(e);
     return SEM_OK;
     GUARD_END
 }

@@ -353,8 +353,12 @@ struct TrainSmem {
     float g[kMlpParams];
 };
 
+// dy_in non-null: the gradient of the output per row is given (dy_in[row]; no loss), otherwise
+// dy = 2 (y - t) / n.  dx_out non-null: the gradient with respect to the (BF16-rounded) inputs,
+// dx[row][k] = sum_n dZ1[row][n] W1[n][k] (k < 81), is written too.
 __global__ void __launch_bounds__(128) k_mlp_train_pass(const MlpDev net, const float *x, const float *t, int64_t n,
-                                                        double *part_loss, float *part)
+                                                        double *part_loss, float *part, const float *dy_in,
+                                                        float *dx_out)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
@@ -382,9 +386,13 @@ __global__ void __launch_bounds__(128) k_mlp_train_pass(const MlpDev net, const 
                     const int64_t row = row0 + r;
                     float d = 0.f;
                     if (row < n) {
-                        const float e = yv[mt][hrow] - t[row];
-                        lsum += (double)e * e;
-                        d = 2.f * e * inv_n;
+                        if (dy_in) {
+                            d = dy_in[row];
+                        } else {
+                            const float e = yv[mt][hrow] - t[row];
+                            lsum += (double)e * e;
+                            d = 2.f * e * inv_n;
+                        }
                     }
                     ts.dy[r] = d;
                 }
@@ -431,6 +439,15 @@ __global__ void __launch_bounds__(128) k_mlp_train_pass(const MlpDev net, const 
             }
 #pragma unroll
             for (int k = 0; k < H; k++) ts.z1[r * H + k] = dh[k] * gelu_d(ts.z1[r * H + k]);
+            if (dx_out && row0 + r < n) {
+                // input gradient of the row from its own dZ1 (this thread's row only)
+                float *dxr = dx_out + (row0 + r) * kMlpIn;
+                for (int k = 0; k < kMlpIn; k++) {
+                    float a = 0.f;
+                    for (int nn = 0; nn < H; nn++) a = fmaf(ts.z1[r * H + nn], bf2f(s.w1[nn * KP1 + k]), a);
+                    dxr[k] = a;
+                }
+            }
         }
         __syncthreads();
         // db1 and dW1[n][k] = sum_r dZ1[r][n] X[r][k] (k < 81)
@@ -481,7 +498,7 @@ __global__ void k_mlp_reduce(const float *part, const double *part_loss, int nb,
 // dw3[c] = sum_r dy[r] GELU(z2[r][c]) needs the forward activations the training pass
 // overwrites; this pass recomputes them (forward only) and accumulates dw3.
 __global__ void __launch_bounds__(128) k_mlp_grad_w3(const MlpDev net, const float *x, const float *t, int64_t n,
-                                                     float *part)
+                                                     float *part, const float *dy_in)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
@@ -507,7 +524,7 @@ __global__ void __launch_bounds__(128) k_mlp_grad_w3(const MlpDev net, const flo
                 for (int hrow = 0; hrow < 2; hrow++) {
                     const int r = w * 32 + mt * 16 + g + hrow * 8;
                     const int64_t row = row0 + r;
-                    dy[r] = row < n ? 2.f * (yv[mt][hrow] - t[row]) * inv_n : 0.f;
+                    dy[r] = row < n ? (dy_in ? dy_in[row] : 2.f * (yv[mt][hrow] - t[row]) * inv_n) : 0.f;
                 }
         __syncthreads();
         if (threadIdx.x < H) {
@@ -887,7 +904,7 @@ cudaError_t mlp_forward(const MlpDev &net, const float *x, float *y, int64_t n, 
 }
 
 cudaError_t mlp_loss_grad(const MlpDev &net, const float *x, const float *t, int64_t n, double *loss, float *grad,
-                          float *part, double *part_loss, cudaStream_t s)
+                          float *part, double *part_loss, cudaStream_t s, const float *dy_in, float *dx_out)
 {
     if (n <= 0) return cudaSuccess;
     const int nb = grid_for(n);
@@ -895,12 +912,12 @@ cudaError_t mlp_loss_grad(const MlpDev &net, const float *x, const float *t, int
     size_t sm = smem_train();
     cudaError_t e = cudaFuncSetAttribute(k_mlp_train_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_mlp_train_pass<<<nb, T, sm, s>>>(net, x, t, n, part_loss, part);
+    k_mlp_train_pass<<<nb, T, sm, s>>>(net, x, t, n, part_loss, part, dy_in, dx_out);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     sm = smem_w3();
     if ((e = cudaFuncSetAttribute(k_mlp_grad_w3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
         return e;
-    k_mlp_grad_w3<<<nb, T, sm, s>>>(net, x, t, n, part);
+    k_mlp_grad_w3<<<nb, T, sm, s>>>(net, x, t, n, part, dy_in);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_mlp_reduce<<<(kMlpParams + 255) / 256, 256, 0, s>>>(part, part_loss, nb, grad, loss);
     return cudaGetLastError();

@@ -6,6 +6,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "host_util.h"
+
 namespace semgb {
 
 constexpr int kMlpIn = 81;
@@ -71,6 +73,44 @@ struct AbcFaceArgs {
 // boundary nodes is taken as s * hist (what the step leaves there), the rest from p_new.
 cudaError_t abc_face(const MlpDev &net, const AbcFaceArgs &a, cudaStream_t s);
 
+// ---- adjoint of the time loop with the network on the boundary nodes (k_bptt.cu) ----------
+// Work arrays of one backward pass over a box (device layout, nb boundary nodes).
+struct BpttFields {
+    int nx, ny, nz;
+    int64_t nxp, n_int;
+    const float *sx, *sy, *sz;  // sponge factors (null: none)
+    const int64_t *nodes;       // boundary nodes (device layout), nb of them
+    int64_t nb;
+    const int *sidx;            // [n_int]: index in `nodes`, -1 elsewhere
+    float *x;                   // [nb][81] features divided by the scale
+    float *scale;               // [nb]
+    int *kstar;                 // [nb] arg-max feature | 0x100 if negative; -1: all zero
+    float *y, *g, *dy;          // [nb] network output, adjoint of the node's new value, output gradient
+    float *dx;                  // [nb][81] input gradient, then feature gradient
+    float *a[3];                // adjoints of out^m, out^{m-1}, out^{m-2}
+    float *v;                   // [n_int] work field
+    const int64_t *roi;         // region of interest (device layout), n_roi nodes
+    int n_roi;
+};
+// The stiffness operator of the stencil pass: 1-D table T[l][d + o] (direct form, diagonal
+// included), assembled weights by local index, g for the x, z and y terms.
+struct BpttOperator {
+    int order;
+    float T[kMaxOrder * (2 * kMaxOrder + 1)];
+    float wa[kMaxOrder];
+    float g[3];
+};
+// Features of the boundary nodes from out^m, out^{m-1}, out^{m-2}.
+cudaError_t bptt_features(const BpttFields &f, const float *lm, const float *lm1, const float *lm2, cudaStream_t s);
+// g and dy from A0 and the network output y.
+cudaError_t bptt_dy(const BpttFields &f, cudaStream_t s);
+// dx -> feature gradient, gathered into A0, A1, A2.
+cudaError_t bptt_scatter(const BpttFields &f, cudaStream_t s);
+// Interior leapfrog adjoint (A0 -> A1, A2); a_mass = dt^2 / M.
+cudaError_t bptt_interior(const BpttFields &f, const BpttOperator &op, const float *a_mass, cudaStream_t s);
+// Loss over the region of interest at one step and its gradient into A0.
+cudaError_t bptt_loss(const BpttFields &f, const float *out, const float *ref, double *loss, cudaStream_t s);
+
 // bf16 conversion of the FP32 master weights into the device layout.
 cudaError_t mlp_pack(const float *master, uint16_t *w1, uint16_t *w2, float *b1, float *b2, float *w3, float *b3,
                      cudaStream_t s);
@@ -81,8 +121,12 @@ cudaError_t mlp_forward(const MlpDev &net, const float *x, float *y, int64_t n, 
 // Deterministic: every CTA writes its partial sums to part ([kMlpMaxCTAs][kMlpParams]) and
 // part_loss ([kMlpMaxCTAs]), and one pass adds them in CTA order.
 constexpr int kMlpMaxCTAs = 152 * 4;
+// With dy_in (device, [n]) the output gradient per row is given instead of the squared-error loss
+// (t is not read and the loss is not accumulated); with dx_out (device, [n][81]) the gradient with
+// respect to the inputs is written too.
 cudaError_t mlp_loss_grad(const MlpDev &net, const float *x, const float *t, int64_t n, double *loss, float *grad,
-                          float *part, double *part_loss, cudaStream_t s);
+                          float *part, double *part_loss, cudaStream_t s, const float *dy_in = nullptr,
+                          float *dx_out = nullptr);
 // bx[i] = x[idx[i]], bt[i] = t[idx[i]] for i < nb (minibatch rows).
 cudaError_t mlp_gather_rows(const float *x, const float *t, const int64_t *idx, int64_t nb, float *bx, float *bt,
                             cudaStream_t s);

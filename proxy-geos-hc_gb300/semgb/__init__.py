@@ -124,6 +124,9 @@ _SIGS = {
     "sem_group_synchronize": [_VP],
     "sem_group_time_step": [_VP, C.c_int, C.POINTER(C.c_float)],
     "sem_group_set_launch": [_VP, C.c_int],
+    "sem_abc_bptt": [_VP, C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_float), C.POINTER(C.c_double),
+                     C.POINTER(C.c_float)],
+    "sem_mlp_adam_step": [_VP, C.POINTER(C.c_float), C.c_float],
     "sem_group_get_launch": [_VP, C.POINTER(C.c_int)],
     "sem_adjoint_create": [_VP, C.c_float, C.c_int, C.c_int, C.POINTER(_VP)],
     "sem_adjoint_destroy": [_VP],
@@ -623,6 +626,12 @@ class Mlp:
                                    _p(losses, _F64P)))
         return losses[:epochs]
 
+    def adam_step(self, grad, lr=1e-3):
+        """One Adam step with a given gradient (e.g. from Abc.bptt)."""
+        g = _f32(grad).reshape(-1)
+        assert g.size == self.n_params
+        _check(lib().sem_mlp_adam_step(self._h, _p(g, _F32P), lr))
+
 
 class Abc:
     """Learned absorbing boundary on a solver (sem_abc_*): after every step the network corrects
@@ -673,6 +682,18 @@ class Abc:
         sc = np.zeros(self.n_nodes, np.float32)
         _check(lib().sem_abc_features(self._h, _p(x, _F32P), _p(sc, _F32P)))
         return x, sc
+
+    def bptt(self, roi_nodes, ref, grad: bool = True):
+        """Loss sum_m sum_r (p^m_r - ref[m-1][r])^2 of n_steps = len(ref) corrected steps from rest
+        and (grad=True) its gradient with respect to the network's parameters through the adjoint
+        of the whole time loop (sem_abc_bptt).  Returns (loss, gradient or None)."""
+        roi = np.ascontiguousarray(np.asarray(roi_nodes, np.int64).reshape(-1))
+        r = _f32(ref).reshape(-1, len(roi))
+        loss = C.c_double()
+        g = np.zeros(self.net.n_params, np.float32) if grad else None
+        _check(lib().sem_abc_bptt(self._h, len(r), len(roi), _p(roi, _I64P), _p(r, _F32P), C.byref(loss),
+                                  _p(g, _F32P) if grad else None))
+        return loss.value, g
 
 
 class Adjoint:

@@ -14,6 +14,10 @@ nodes (the correction that would have reproduced the padded run).
 Evaluation: T runs from rest with and without the network; the reflected energy is the sum over
 steps and the nodes of the region of interest of (p_T - p_P)^2, divided by the same sum of p_P^2.
 Set-ups with different sponges around the same region of interest compare directly.
+
+Training through the adjoint (train_through_adjoint): the reflected energy of a whole run of T
+is itself the loss, its gradient with respect to the network's parameters comes from the adjoint
+of the time loop (sem_abc_bptt), and Adam steps follow it.
 """
 from __future__ import annotations
 
@@ -191,6 +195,71 @@ def train_network(s: Setup, net: Mlp, rounds: int = 3, epochs: int = 12, per_ste
         net.params = best[1]
         log.append({"selected_round": best[2], "reflected_energy": best[0]})
     return log
+
+
+def train_through_adjoint(s: Setup, net: Mlp, iters: int = 20, step: float = 0.01, lr: float = 1e-3,
+                          method: str = "line", keep_best: bool = True):
+    """Trains the network on the reflected energy itself, through the adjoint of the whole time
+    loop.  Every evaluation runs T with the network from rest (s.steps steps); the loss is
+    sum over steps and region-of-interest nodes of (p_T - p_P)^2 / sum p_P^2 (the padded run P
+    restricted to T), and its gradient with respect to the network's parameters comes from the
+    adjoint pass (sem_abc_bptt: the network's backward kernels at the boundary nodes and the
+    adjoint leapfrog of the stencil pass).  Layer 0 only.
+
+    method "line": steepest descent with a search along the normalised negative gradient (steps
+    step * 2^k, k = -2..2, the best kept; `step` follows the accepted one, halved when none
+    lowers the loss): a 260-step rollout makes the loss rough, and a search along the exact
+    gradient never accepts a step that raises it.  method "adam": one Adam step of rate `lr` per
+    gradient.  With keep_best the parameters of the lowest loss seen are kept.  Returns the
+    loss after every iteration (entry 0: before training)."""
+    if s.layer != 0:
+        raise ValueError("training through the adjoint needs the network on the boundary nodes (layer 0)")
+    (mt, st), (mp, sp) = make_solvers(s)
+    mask = interior_mask(s)
+    roi = np.nonzero(mask)[0]
+    ref = np.empty((s.steps, len(roi)), np.float32)
+    for n in range(s.steps):
+        sp.step(1)
+        ref[n] = restrict(s, sp.pressure(LEVEL_CURRENT))[mask]
+    den = max(float(np.sum(ref.astype(np.float64) ** 2)), 1e-300)
+    abc = Abc(st, net, 0)
+
+    def loss_at(p):
+        net.params = p
+        return abc.bptt(roi, ref, grad=False)[0] / den
+
+    theta = net.params.copy()
+    history = []
+    best = (np.inf, theta.copy())
+    for it in range(iters + 1):
+        net.params = theta
+        loss, g = abc.bptt(roi, ref, grad=it < iters)
+        e = loss / den
+        history.append(e)
+        if e < best[0]:
+            best = (e, theta.copy())
+        if it == iters:
+            break
+        if method == "adam":
+            net.adam_step(g / den, lr)
+            theta = net.params.copy()
+            continue
+        d = -g.astype(np.float64)
+        nrm = float(np.linalg.norm(d))
+        if not np.isfinite(nrm) or nrm == 0.0:
+            break
+        d = (d / nrm).astype(np.float32)
+        tried = [(loss_at(theta + step * (2.0 ** k) * d), k) for k in (-2, -1, 0, 1, 2)]
+        lk, k = min(tried)
+        if lk < e:
+            theta = theta + step * (2.0 ** k) * d
+            step *= 2.0 ** k
+        else:
+            step *= 0.25
+    net.params = best[1] if keep_best else theta
+    for o in (abc, st, sp, mt, mp):
+        o.close()
+    return history
 
 
 def interior_mask(s: Setup):

@@ -80,6 +80,98 @@ def test_training_is_reproducible(semgb_lib, cuda_device):
     assert runs[0][2] == runs[1][2] and np.array_equal(runs[0][3], runs[1][3])
 
 
+def _bptt_setup(semgb, layer_seed=3, steps=70):
+    from semgb import learned_boundary as LB
+    from semgb import workloads as W
+    c, h, o = 2000.0, 10.0, 2
+    dt = W.cfl_dt(h, o, c)
+    s = LB.Setup(interior=2, sponge_t=1, order=o, h=h, c=c, pad=3, sponge_p=2, layer=0, f0=120.0, dt=dt,
+                 steps=steps, src_frac=(0.5, 0.5, 0.5))
+    (mt, st), (mp, sp) = LB.make_solvers(s)
+    net = semgb.Mlp(layer_seed)
+    net.params = _params(11, 0.02)
+    abc = semgb.Abc(st, net, 0)
+    roi = np.nonzero(LB.interior_mask(s))[0]
+    return s, (mt, st, mp, sp), net, abc, roi
+
+
+def test_bptt_loss_matches_forward_run(semgb_lib, cuda_device):
+    """The loss the adjoint pass reports is that of the ordinary corrected run from rest."""
+    semgb = semgb_lib
+    s, (mt, st, mp, sp), net, abc, roi = _bptt_setup(semgb)
+    ref = np.random.default_rng(4).standard_normal((s.steps, len(roi))).astype(np.float32) * 1e-4
+    loss, _ = abc.bptt(roi, ref, grad=False)
+    st.reset()
+    abc.reset()
+    want = 0.0
+    for m in range(s.steps):
+        abc.step(1)
+        p = st.pressure()[roi].astype(np.float64)
+        want += float(np.sum((p - ref[m]) ** 2))
+    assert abs(loss - want) <= 1e-5 * want
+    for o in (abc, net, st, sp, mt, mp):
+        o.close()
+
+
+def test_bptt_gradient_matches_central_differences(semgb_lib, cuda_device):
+    """Gradient of a loss over the region of interest through the adjoint of the whole time loop
+    (network on the boundary nodes) against central differences of the loss, along seeded random
+    directions in the FP32 parameters (hidden biases, output weights and bias; the BF16 weight
+    matrices round small steps away, their gradient given the output gradient is pinned to the
+    oracle above), FP64 loss sums."""
+    semgb = semgb_lib
+    s, (mt, st, mp, sp), net, abc, roi = _bptt_setup(semgb)
+    ref = np.zeros((s.steps, len(roi)), np.float32)
+    p0 = net.params.copy()
+    loss, g = abc.bptt(roi, ref)
+    assert loss > 0 and np.all(np.isfinite(g))
+    n_w1, h = 64 * 81, 64
+    fp32 = np.r_[np.arange(n_w1, n_w1 + h), np.arange(n_w1 + h + h * h, len(p0))]  # b1, b2, w3, b3
+    rng = np.random.default_rng(9)
+    errs = []
+    for _ in range(3):
+        v = np.zeros_like(p0)
+        v[fp32] = rng.standard_normal(len(fp32)).astype(np.float32)
+        eps = 1e-2
+        lp = []
+        for sign in (1.0, -1.0):
+            net.params = p0 + sign * eps * v
+            lp.append(abc.bptt(roi, ref, grad=False)[0])
+        net.params = p0
+        fd = (lp[0] - lp[1]) / (2 * eps)
+        ad = float(np.dot(g.astype(np.float64), v.astype(np.float64)))
+        errs.append(abs(fd - ad) / max(abs(fd), 1e-30))
+        print(f"directional derivative: central differences {fd:.6e}, adjoint {ad:.6e}")
+    assert max(errs) < 2e-2, errs
+    for o in (abc, net, st, sp, mt, mp):
+        o.close()
+
+
+def test_training_through_the_adjoint_lowers_reflections(semgb_lib, cuda_device):
+    """Steepest descent on the reflected energy of whole runs, with the gradient from the adjoint
+    of the time loop, starting from a network trained on samples: the loss falls (the search
+    never accepts a step that raises it) and the reflected energy of a held-out source falls too."""
+    semgb = semgb_lib
+    from semgb import learned_boundary as LB
+    from semgb import workloads as W
+    c, h, o = 2000.0, 10.0, 2
+    dt = W.cfl_dt(h, o, c)
+    common = dict(interior=6, sponge_t=2, order=o, h=h, c=c, pad=8, sponge_p=4, layer=0, f0=60.0, dt=dt, steps=200)
+    s = LB.Setup(src_frac=(0.3, 0.5, 0.5), **common)
+    held = LB.Setup(src_frac=(0.6, 0.4, 0.55), **common)
+    net = semgb.Mlp(5)
+    LB.train_network(s, net, rounds=1, epochs=8, per_step=2000, seed=0)
+    h0 = LB.reflected_energy(held, net)[0]
+    hist = LB.train_through_adjoint(s, net, iters=8)
+    h1 = LB.reflected_energy(held, net)[0]
+    print(f"adjoint training: loss {hist[0]:.4e} -> {min(hist):.4e}; held-out source {h0:.4e} -> {h1:.4e}")
+    # (the loss with a gradient is summed newest step first: equal losses can differ in the last bit)
+    assert all(b <= a * (1 + 1e-9) for a, b in zip(hist, hist[1:]))
+    assert min(hist) < 0.8 * hist[0]
+    assert h1 < h0
+    net.close()
+
+
 def _solver(semgb, wl):
     mesh, s = semgb.solver_from_workload(wl, semgb.KERNEL_STENCIL)
     return mesh, s
