@@ -64,6 +64,8 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sh_addr(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until none of this thread's copies is in flight
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 // wait until at most one group (the most recent) of this thread is still in flight
 __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
@@ -158,8 +160,13 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
     // Persistent loop: while a tile runs its z- and y-directions and its scatter, the next
     // tile's connectivity rows are in shared memory and its pencil values are in flight, and the
     // rows of the tile after it are being copied.  Buffer b holds this tile's rows, bn the
-    // next tile's, bf the one after (last used by the previous tile, whose final barrier has
-    // passed).
+    // next tile's, bf the one after (last read by the previous tile's scatter).  Two barriers
+    // per tile: (1) after the pencil values are stored -- every warp has also finished the
+    // previous tile's scatter, so bf and the z/y result buffers are free, and the copies of the
+    // next tile's rows have landed; (2) after the z- and y-directions.  The pencil values of the
+    // next tile are stored after barrier 2 of this one, when no warp reads them any more.  The
+    // reference-rounding form reads the pencil values after barrier 1 and keeps a third barrier
+    // at the end of the tile, with the copies issued before barrier 1.
     for (int b = 0; t < ntiles; t += gridDim.x, b = b == 2 ? 0 : b + 1) {
         const int64_t tn = t + gridDim.x;
         const int bn = b == 2 ? 0 : b + 1, bf = bn == 2 ? 0 : bn + 1;
@@ -171,7 +178,7 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
             px[i] = pn[i];
             s_p[(i + O1 * jx + NP * kx) * TE + lane] = px[i];
         }
-        load_conn(tn + gridDim.x, bf);
+        if constexpr (REF) load_conn(tn + gridDim.x, bf);
         float yx[O1];
         if constexpr (REF) {
             cp_async_wait_one();  // the next tile's rows (all but the copies just issued)
@@ -204,8 +211,9 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
         } else {
             // C: x-direction in registers
             pencil_apply<O>(a, px, s_tab[0 * NP + jx + O1 * kx], yx);
-            cp_async_wait_one();  // the next tile's rows (all but the copies just issued)
+            cp_async_wait_all();  // the next tile's rows
             __syncthreads();
+            load_conn(tn + gridDim.x, bf);
             if (tn < ntiles) gather(tn, bn, pn);
             // D: z-direction (local index j varies) into s_y, and E: y-direction (local index k
             // varies) into s_w; both only read s_p, so no barrier between them
@@ -259,8 +267,9 @@ __global__ void __launch_bounds__(ElemCfg<O>::THREADS, ElemCfg<O>::MINB)
                 }
             }
         }
-        __syncthreads();  // s_p, s_y, s_w and this tile's rows are reused by the next iteration
+        if constexpr (REF) __syncthreads();  // s_p and this tile's rows are reused by the next iteration
     }
+    cp_async_wait_all();  // no copy left in flight into shared memory
 }
 
 template <int O, bool REF, bool CHECKED = false>
