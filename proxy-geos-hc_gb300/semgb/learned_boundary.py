@@ -229,6 +229,7 @@ def train_through_adjoint(s: Setup, net: Mlp, iters: int = 20, step: float = 0.0
         return abc.bptt(roi, ref, grad=False)[0] / den
 
     theta = net.params.copy()
+    step0 = step
     history = []
     best = (np.inf, theta.copy())
     for it in range(iters + 1):
@@ -256,6 +257,8 @@ def train_through_adjoint(s: Setup, net: Mlp, iters: int = 20, step: float = 0.0
             step *= 2.0 ** k
         else:
             step *= 0.25
+            if step < step0 * 1e-3:
+                step = step0  # no progress at any step length: search again from the start
     net.params = best[1] if keep_best else theta
     for o in (abc, st, sp, mt, mp):
         o.close()
