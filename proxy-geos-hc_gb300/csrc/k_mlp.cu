@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 #include <cstddef>
 
 #include "mlp.h"
@@ -938,19 +939,44 @@ cudaError_t mlp_gather_rows(const float *x, const float *t, const int64_t *idx, 
     return cudaGetLastError();
 }
 
+// Per-device launch set-up of a boundary kernel: its shared-memory limit is raised, and the
+// resident CTAs of the device (SMs x CTAs per SM) recorded, once per device.
+struct DeviceLaunch {
+    int dev;
+    int resident;
+};
+
+template <class K>
+cudaError_t resident_ctas(K kernel, size_t sm, std::vector<DeviceLaunch> &cache, int &resident)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    for (const DeviceLaunch &d : cache)
+        if (d.dev == dev) { resident = d.resident; return cudaSuccess; }
+    if ((e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess) return e;
+    int sms = 152, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, T, sm) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    resident = sms * per_sm;
+    cache.push_back({dev, resident});
+    return cudaSuccess;
+}
+
 cudaError_t abc_correction(const MlpDev &net, const AbcArgs &a, cudaStream_t s)
 {
     if (a.n <= 0) return cudaSuccess;
     const size_t sm = smem_abc();
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_abc_correction, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
-    // persistent CTAs (four per SM fit the shared memory): the weights are staged once per CTA
+    static std::vector<DeviceLaunch> cache;
+    int resident = 0;
+    cudaError_t e = resident_ctas(k_abc_correction, sm, cache, resident);
+    if (e != cudaSuccess) return e;
+    // persistent CTAs, as many as are resident at once: the weights are staged once per CTA
     const int64_t tiles = (a.n + T - 1) / T;
-    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, 152 * 4), T, sm, s>>>(net, a);
+    k_abc_correction<<<(unsigned)std::min<int64_t>(tiles, resident), T, sm, s>>>(net, a);
     return cudaGetLastError();
 }
 
@@ -958,24 +984,12 @@ cudaError_t abc_face(const MlpDev &net, const AbcFaceArgs &a, cudaStream_t s)
 {
     if (a.ntiles <= 0) return cudaSuccess;
     const size_t sm = smem_face();
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_abc_face, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static std::vector<DeviceLaunch> cache;
+    int resident = 0;
+    cudaError_t e = resident_ctas(k_abc_face, sm, cache, resident);
+    if (e != cudaSuccess) return e;
     // persistent CTAs, as many as are resident at once (the weights are staged once per CTA)
-    static int per_sm = 0, sms = 0;
-    if (per_sm == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_abc_face, T, sm) != cudaSuccess || per_sm < 1) {
-            cudaGetLastError();
-            per_sm = 1;
-        }
-    }
-    k_abc_face<<<(unsigned)std::min<int64_t>(a.ntiles, (int64_t)sms * per_sm), T, sm, s>>>(net, a);
+    k_abc_face<<<(unsigned)std::min<int64_t>(a.ntiles, resident), T, sm, s>>>(net, a);
     return cudaGetLastError();
 }
 

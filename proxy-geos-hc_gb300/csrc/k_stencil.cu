@@ -36,8 +36,7 @@ template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF = fals
 __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
     k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap win_map,
               const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap a_map,
-              const __grid_constant__ StencilTables t, const __grid_constant__ StencilArgs a,
-              const __grid_constant__ ClassParam<O, REF> ct)
+              const StencilTables t, const StencilArgs a, const __grid_constant__ ClassParam<O, REF> ct)
 {
     // CTA -> (x-tile, z-tile, y-chunk): grid (x-tiles, z-tiles, chunks).  MULTI (many shots, the
     // levels stacking the shots along y: plane p of shot s is plane s*ny + p): grid

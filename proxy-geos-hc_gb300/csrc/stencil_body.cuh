@@ -402,16 +402,25 @@ __device__ __forceinline__ void stencil_cta(const CUtensorMap *rmap, const CUten
     const float wz = c_wa[O - 1][lz];
     const int off = (rw + O) * TXP + HX + O * xl;  // offset of the thread's first node in the window
     const int toff = rw * TX + O * xl;             // in-tile offset (aux tiles, y-ring slots)
-    float *dst_col = a.prev + (MULTI ? (int64_t)shot * t.shot_stride : 0) + (int64_t)xb + (int64_t)z * t.nxp;
-    const int64_t plane_stride = t.nxp * t.nz;
-    const int64_t group_stride = (int64_t)GR * t.nxp;
+    // loop-invariant fields of the tables and arguments, read once: the level stores below cannot
+    // change them, which the compiler cannot tell through the references
+    const float tg0 = t.g[0], tg1 = t.g[1], tg2 = t.g[2];
+    const int64_t nxp = t.nxp;
+    const float *const a_sy = a.sy;
+    float *const a_kp = a.kp;
+    float *const a_grad = a.grad;
+    int *const a_status = a.status;
+    float *const a_prev = a.prev;
+    float *dst_col = a_prev + (MULTI ? (int64_t)shot * t.shot_stride : 0) + (int64_t)xb + (int64_t)z * nxp;
+    const int64_t plane_stride = nxp * t.nz;
+    const int64_t group_stride = (int64_t)GR * nxp;
 
     bool ok = true;
     for (int p = yb - O; p < yb + O; p++) {
         const int i = p - yb + O;  // < 2O < R: first fill of each of these slots
         ok &= bar_wait(bars + i, 0, kWaitLimitNs);
     }
-    if (!ok) atomicExch(a.status, 1);
+    if (!ok) atomicExch(a_status, 1);
     bool aborted = __syncthreads_or(!ok) != 0;
 
     // all nodes of the thread strictly inside the mesh along x and z: no per-node checks on the
@@ -444,12 +453,12 @@ __device__ __forceinline__ void stencil_cta(const CUtensorMap *rmap, const CUten
         // before the waits so that their latency overlaps the plane's work
         float kpv[NG][O], grv[NG][O];
         if constexpr (MODE == STENCIL_GRADIENT) {
-            const int64_t so = (dst_col - a.prev) + (int64_t)y * plane_stride;
+            const int64_t so = (dst_col - a_prev) + (int64_t)y * plane_stride;
 #pragma unroll
             for (int g = 0; g < NG; g++) {
                 if (row_ok[g]) {
-                    load_o_lim<O>(a.kp + so + g * group_stride, kpv[g], (int)t.nxp - xb);
-                    load_o_lim<O>(a.grad + so + g * group_stride, grv[g], (int)t.nxp - xb);
+                    load_o_lim<O>(a_kp + so + g * group_stride, kpv[g], (int)nxp - xb);
+                    load_o_lim<O>(a_grad + so + g * group_stride, grv[g], (int)nxp - xb);
                 } else {
 #pragma unroll
                     for (int j = 0; j < O; j++) kpv[g][j] = grv[g][j] = 0.f;
@@ -458,7 +467,7 @@ __device__ __forceinline__ void stencil_cta(const CUtensorMap *rmap, const CUten
         }
         ok = bar_wait(bars + ws, wph, kWaitLimitNs);
         ok &= bar_wait(bars + R + as, aph, kWaitLimitNs);
-        if (!ok) atomicExch(a.status, 1);
+        if (!ok) atomicExch(a_status, 1);
         {
             // rows past the mesh read zero-filled shared memory; only their stores are skipped
             const float *cur = aux + as * C::AUX_FLOATS + 2 * C::TILE_FLOATS + off;  // window
@@ -517,8 +526,8 @@ __device__ __forceinline__ void stencil_cta(const CUtensorMap *rmap, const CUten
 
             const bool yin = y > 0 && y < ny - 1;
             const float wy = c_wa[O - 1][ly];
-            const float syv = SPONGE ? __ldg(a.sy + y) : 1.f;
-            const float gx = t.g[0] * (wz * wy), gzy = t.g[1] * wy, gyz = t.g[2] * wz;
+            const float syv = SPONGE ? __ldg(a_sy + y) : 1.f;
+            const float gx = tg0 * (wz * wy), gzy = tg1 * wy, gyz = tg2 * wz;
             float *dst = dst_col + (int64_t)y * plane_stride;
             float out[NG][O], kp[NG][O], sv[NG][O], qdv[NG][O];
             if constexpr (SEM_STENCIL_PACKED && O > 1) {
@@ -608,21 +617,21 @@ __device__ __forceinline__ void stencil_cta(const CUtensorMap *rmap, const CUten
                 if (MODE != STENCIL_PLAIN) {
                     // side buffers: same device layout as the levels (padding columns hold zeros:
                     // K p' is 0 there and the gradient keeps its value)
-                    const int64_t so = dg - a.prev;
+                    const int64_t so = dg - a_prev;
                     if (MODE == STENCIL_GRADIENT)
 #pragma unroll
                         for (int j = 0; j < O; j++) kp[g][j] = fmaf(c[g][j], kpv[g][j], grv[g][j]);
-                    store_o_lim<O>((MODE == STENCIL_GRADIENT ? a.grad : a.kp) + so, kp[g], (int)t.nxp - xb);
+                    store_o_lim<O>((MODE == STENCIL_GRADIENT ? a_grad : a_kp) + so, kp[g], (int)nxp - xb);
                 }
                 if constexpr (O == 4) {
-                    if (xb + 4 <= t.nxp)
+                    if (xb + 4 <= nxp)
                         *reinterpret_cast<float4 *>(dg) = make_float4(out[g][0], out[g][1], out[g][2], out[g][3]);
                 } else if constexpr (O == 2) {
-                    if (xb + 2 <= t.nxp) *reinterpret_cast<float2 *>(dg) = make_float2(out[g][0], out[g][1]);
+                    if (xb + 2 <= nxp) *reinterpret_cast<float2 *>(dg) = make_float2(out[g][0], out[g][1]);
                 } else {
 #pragma unroll
                     for (int j = 0; j < O; j++)
-                        if (xb + j < t.nxp) dg[j] = out[g][j];
+                        if (xb + j < nxp) dg[j] = out[g][j];
                 }
             }
         }
