@@ -719,7 +719,8 @@ def run_case(name: str):
     """Small fixed cases for kernel profiles (no JSON line): `batch40` steps a 64-shot batch on a
     40^3 Q4 mesh 6 times; `abc86` runs 6 steps of an 86^3 Q4 mesh with the boundary network;
     `q5_80` runs 6 stencil steps of an 80^3 order-5 box (401^3 nodes, constant 2000 m/s,
-    20-element sponge, one source)."""
+    20-element sponge, one source); `uneven_small` steps the 32 small uneven problems (8-24
+    elements per axis, orders 2-4) as one group 6 times."""
     import semgb
     from semgb import workloads as W
     if name == "batch40":
@@ -760,6 +761,17 @@ def run_case(name: str):
         sol.step(6)
         sol.synchronize()
         print("q5_80 ok", mesh.n_nodes)
+    elif name == "uneven_small":
+        wls = W.c3_uneven_batch(32, 800, lo=8, hi=24)
+        members = [semgb.solver_from_workload(w, semgb.KERNEL_STENCIL) for w in wls]
+        g = semgb.Group([s for _, s in members])
+        g.step(6)
+        g.synchronize()
+        print("uneven_small ok", sum(m.n_nodes for m, _ in members), "one launch:", g.launch == semgb.GROUP_ONE_LAUNCH)
+        g.close()
+        for m, s in members:
+            s.close()
+            m.close()
     else:
         raise SystemExit(f"unknown case {name}")
 
@@ -779,7 +791,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=6, help="cpu_baseline steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-rows", action="store_true", help="skip the element-path / batched / uneven / adjoint / learned-boundary rows")
-    ap.add_argument("--case", choices=["batch40", "abc86", "q5_80"], default=None,
+    ap.add_argument("--case", choices=["batch40", "abc86", "q5_80", "uneven_small"], default=None,
                     help="run a small fixed case for a kernel profile instead of the benchmark")
     args = ap.parse_args()
     if args.case:
