@@ -449,7 +449,10 @@ int sem_abc_features(sem_abc *a, float *x, float *scale);
  * parameters is computed by the adjoint of every step, newest first: the network's own backward
  * kernels at the boundary nodes (through the division by the neighbourhood's largest magnitude
  * and the clipping) and the adjoint leapfrog of the stencil pass, from the recorded levels.
- * Sources must lie at least two nodes inside the box.  The solver is left after the n_steps. */
+ * Sources must lie at least two nodes inside the box.  The solver is left after the n_steps.
+ * Every level is recorded: (n_steps + 2) x (the mesh's device-layout node count) floats of
+ * device memory, plus a few fields, for the duration of the call (meant for training regions;
+ * SEM_ERR_OOM when it does not fit). */
 int sem_abc_bptt(sem_abc *a, int n_steps, int n_roi, const int64_t *roi_nodes, const float *ref, double *loss,
                  float *grad);
 
