@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <numeric>
+#include <utility>
 #include <vector>
 
 #include "abi.h"
@@ -132,9 +133,10 @@ int capture(sem_group *g, int parity)
 }
 
 // y-chunk length of every member for one launch over the group: chunks of about L planes, L
-// chosen to minimise max(total work / resident CTAs, longest CTA), the work of a CTA being its
-// planes plus the 2o planes it reads before its first output (longest CTAs run first, so the
-// last wave is no longer than the longest CTA).
+// chosen to minimise the launch's makespan, estimated by placing the CTAs longest first on the
+// resident CTA slots, each on the least loaded one (a member's CTAs all have the same work, so
+// they go in whole rounds over the slots, the remainder on the least loaded); a CTA's work is
+// its planes plus the 2o planes it reads before its first output.
 std::vector<int> group_chunks(const sem_group *g, int64_t resident)
 {
     const size_t n = g->members.size();
@@ -142,17 +144,29 @@ std::vector<int> group_chunks(const sem_group *g, int64_t resident)
     for (const sem_solver *s : g->members) ny_max = std::max(ny_max, s->mesh->box.ny);
     double best = 1e300;
     int64_t best_l = ny_max;
+    std::vector<std::pair<int64_t, int64_t>> jobs;  // (CTA work in planes, CTA count)
+    std::vector<double> load((size_t)std::max<int64_t>(resident, 1));
     for (int64_t L = 1; L <= ny_max; L++) {
-        double work = 0, longest = 0;
+        jobs.clear();
         for (const sem_solver *s : g->members) {
             const Box &b = s->mesh->box;
             const int64_t cols = (int64_t)s->stencil->grid[0] * s->stencil->grid[1];
             const int64_t c = (b.ny + L - 1) / L, chunk = (b.ny + c - 1) / c;
-            work += (double)cols * c * (chunk + 2 * b.order);
-            longest = std::max(longest, (double)(chunk + 2 * b.order));
+            jobs.push_back({chunk + 2 * b.order, cols * c});
         }
-        const double cost = std::max(work / (double)resident, longest);
-        if (cost < best - 1e-9) { best = cost; best_l = L; }
+        std::sort(jobs.begin(), jobs.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
+        std::fill(load.begin(), load.end(), 0.0);  // kept in ascending order
+        const int64_t R = (int64_t)load.size();
+        for (const auto &jb : jobs) {
+            const double w = (double)jb.first;
+            const int64_t rounds = jb.second / R, rem = jb.second % R;
+            if (rounds > 0)
+                for (double &x : load) x += w * (double)rounds;
+            for (int64_t k = 0; k < rem; k++) load[k] += w;
+            std::inplace_merge(load.begin(), load.begin() + rem, load.end());
+        }
+        const double makespan = load.back();
+        if (makespan < best - 1e-9) { best = makespan; best_l = L; }
     }
     std::vector<int> out(n);
     for (size_t i = 0; i < n; i++) {
