@@ -124,3 +124,26 @@ def test_one_launch_many_tiles_and_chunks(semgb_lib, cuda_device):
     assert g.launch == semgb.GROUP_ONE_LAUNCH
     _same(solo, grouped, semgb)
     _close(grouped, g)
+
+
+@pytest.mark.parametrize("launch", [0, 1], ids=["one_launch", "branches"])
+def test_group_across_trace_growth(semgb_lib, cuda_device, launch):
+    """More steps than the members' first trace storage (64 steps): the storage grows between
+    group steps, the group rebuilds its launch state, and the members still match solo runs."""
+    semgb = semgb_lib
+    n = 150
+    shapes = SHAPES[:3]
+    solo = _members(semgb, n, shapes)
+    for _, s in solo:
+        s.step(n)
+    grouped = _members(semgb, n, shapes)
+    g = semgb.Group([s for _, s in grouped], launch=launch)
+    g.step(50)
+    g.step(31)
+    g.step(69)
+    g.synchronize()
+    _same(solo, grouped, semgb)
+    _close(grouped, g)
+    for m, s in solo:
+        s.close()
+        m.close()
