@@ -197,36 +197,52 @@ def train_network(s: Setup, net: Mlp, rounds: int = 3, epochs: int = 12, per_ste
     return log
 
 
-def train_through_adjoint(s: Setup, net: Mlp, iters: int = 20, step: float = 0.01, lr: float = 1e-3,
+def train_through_adjoint(s, net: Mlp, iters: int = 20, step: float = 0.01, lr: float = 1e-3,
                           method: str = "line", keep_best: bool = True):
     """Trains the network on the reflected energy itself, through the adjoint of the whole time
-    loop.  Every evaluation runs T with the network from rest (s.steps steps); the loss is
-    sum over steps and region-of-interest nodes of (p_T - p_P)^2 / sum p_P^2 (the padded run P
-    restricted to T), and its gradient with respect to the network's parameters comes from the
-    adjoint pass (sem_abc_bptt: the network's backward kernels at the boundary nodes and the
-    adjoint leapfrog of the stencil pass).  Layer 0 only.
+    loop.  `s` is one Setup or a list of Setups (e.g. several source positions around the same
+    region of interest: the loss is then the mean of theirs).  Every evaluation runs T with the
+    network from rest (s.steps steps); a set-up's loss is sum over steps and region-of-interest
+    nodes of (p_T - p_P)^2 / sum p_P^2 (the padded run P restricted to T), and its gradient with
+    respect to the network's parameters comes from the adjoint pass (sem_abc_bptt: the
+    network's backward kernels at the boundary nodes and the adjoint leapfrog of the stencil
+    pass).  Layer 0 only.
 
     method "line": steepest descent with a search along the normalised negative gradient (steps
-    step * 2^k, k = -2..2, the best kept; `step` follows the accepted one, halved when none
-    lowers the loss): a 260-step rollout makes the loss rough, and a search along the exact
-    gradient never accepts a step that raises it.  method "adam": one Adam step of rate `lr` per
-    gradient.  With keep_best the parameters of the lowest loss seen are kept.  Returns the
-    loss after every iteration (entry 0: before training)."""
-    if s.layer != 0:
+    step * 2^k, k = -2..2, the best kept; `step` follows the accepted one, quartered when none
+    lowers the loss and reset when it has shrunk a thousandfold): a 260-step rollout makes the
+    loss rough, and a search along the exact gradient never accepts a step that raises it.
+    method "adam": one Adam step of rate `lr` per gradient.  With keep_best the parameters of
+    the lowest loss seen are kept.  Returns the loss after every iteration (entry 0: before
+    training)."""
+    setups = list(s) if isinstance(s, (list, tuple)) else [s]
+    if any(x.layer != 0 for x in setups):
         raise ValueError("training through the adjoint needs the network on the boundary nodes (layer 0)")
-    (mt, st), (mp, sp) = make_solvers(s)
-    mask = interior_mask(s)
-    roi = np.nonzero(mask)[0]
-    ref = np.empty((s.steps, len(roi)), np.float32)
-    for n in range(s.steps):
-        sp.step(1)
-        ref[n] = restrict(s, sp.pressure(LEVEL_CURRENT))[mask]
-    den = max(float(np.sum(ref.astype(np.float64) ** 2)), 1e-300)
-    abc = Abc(st, net, 0)
+    runs = []  # (roi, ref, den, abc, objects to close)
+    for x in setups:
+        (mt, st), (mp, sp) = make_solvers(x)
+        mask = interior_mask(x)
+        roi = np.nonzero(mask)[0]
+        ref = np.empty((x.steps, len(roi)), np.float32)
+        for n in range(x.steps):
+            sp.step(1)
+            ref[n] = restrict(x, sp.pressure(LEVEL_CURRENT))[mask]
+        den = max(float(np.sum(ref.astype(np.float64) ** 2)), 1e-300)
+        abc = Abc(st, net, 0)
+        runs.append((roi, ref, den, abc, (abc, st, sp, mt, mp)))
+
+    def evaluate(grad: bool):
+        loss, g = 0.0, None
+        for roi, ref, den, abc, _ in runs:
+            l, gg = abc.bptt(roi, ref, grad=grad)
+            loss += l / den / len(runs)
+            if grad:
+                g = gg.astype(np.float64) / den / len(runs) if g is None else g + gg.astype(np.float64) / den / len(runs)
+        return loss, g
 
     def loss_at(p):
         net.params = p
-        return abc.bptt(roi, ref, grad=False)[0] / den
+        return evaluate(False)[0]
 
     theta = net.params.copy()
     step0 = step
@@ -234,18 +250,17 @@ def train_through_adjoint(s: Setup, net: Mlp, iters: int = 20, step: float = 0.0
     best = (np.inf, theta.copy())
     for it in range(iters + 1):
         net.params = theta
-        loss, g = abc.bptt(roi, ref, grad=it < iters)
-        e = loss / den
+        e, g = evaluate(it < iters)
         history.append(e)
         if e < best[0]:
             best = (e, theta.copy())
         if it == iters:
             break
         if method == "adam":
-            net.adam_step(g / den, lr)
+            net.adam_step(g.astype(np.float32), lr)
             theta = net.params.copy()
             continue
-        d = -g.astype(np.float64)
+        d = -g
         nrm = float(np.linalg.norm(d))
         if not np.isfinite(nrm) or nrm == 0.0:
             break
@@ -260,8 +275,9 @@ def train_through_adjoint(s: Setup, net: Mlp, iters: int = 20, step: float = 0.0
             if step < step0 * 1e-3:
                 step = step0  # no progress at any step length: search again from the start
     net.params = best[1] if keep_best else theta
-    for o in (abc, st, sp, mt, mp):
-        o.close()
+    for *_, objs in runs:
+        for o in objs:
+            o.close()
     return history
 
 
