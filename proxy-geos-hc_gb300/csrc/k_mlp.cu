@@ -20,6 +20,19 @@ namespace semgb {
 
 namespace {
 
+// Fragment loads of the register-resident inference forward (compile-time knob: 1 = ldmatrix,
+// 0 = one 32-bit shared load per fragment register; the same fragments either way, so the same
+// bits).  ldmatrix: a quarter of the load instructions, 162 registers, no spill.
+#ifndef SEM_MLP_LDSM
+#define SEM_MLP_LDSM 1
+#endif
+// Face kernel staging (compile-time knob: 1 = the next tile's patch loads issued into registers
+// before the current tile's network runs, stored to shared memory after it; 0 = load and store
+// each tile's patch before its features).  The same values either way.
+#ifndef SEM_MLP_FACE_PIPE
+#define SEM_MLP_FACE_PIPE 1
+#endif
+
 constexpr int H = kMlpHidden;
 constexpr int KP1 = kMlpInPad + 8;  // row stride (bf16) of X and W1
 constexpr int KP2 = H + 8;          // row stride (bf16) of H1 and W2
@@ -89,6 +102,23 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
+
+#if SEM_MLP_LDSM
+// 8x8 b16 matrices from shared memory (fragment layout of the mma operands): x4 takes row
+// addresses from lanes 0-31 (matrix lane/8), x2 from lanes 0-15.
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(static_cast<uint32_t>(__cvta_generic_to_shared(p))));
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const void *p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0, %1}, [%2];"
+                 : "=r"(r[0]), "=r"(r[1])
+                 : "r"(static_cast<uint32_t>(__cvta_generic_to_shared(p))));
+}
+#endif
 
 struct NetSmem {
     uint16_t w1[H * KP1];
@@ -229,7 +259,15 @@ __device__ void forward_rows(const NetSmem &s, const uint16_t *xs, uint16_t *h1,
 // forward_rows.
 __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, float (&yv)[2][2])
 {
-    const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    const int lane = threadIdx.x & 31, q = lane & 3;
+#if SEM_MLP_LDSM
+    // ldmatrix row addresses: A (rows of xs) {rows 0-7, 8-15} x {cols 0-7, 8-15}; B (rows n of
+    // W) {cols 0-7, 8-15} of one n-tile
+    const int a_row = (lane & 7) + ((lane >> 3) & 1) * 8, a_col = (lane >> 4) * 8;
+    const int b_row = lane & 7, b_col = ((lane >> 3) & 1) * 8;
+#else
+    const int g = lane >> 2;
+#endif
     float acc[2][8][4];
 #pragma unroll
     for (int mt = 0; mt < 2; mt++)
@@ -240,20 +278,31 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
 #pragma unroll
     for (int ks = 0; ks < kMlpInPad / 16; ks++) {
         uint32_t a[2][4];
+#if !SEM_MLP_LDSM
         const int k0 = ks * 16 + q * 2;
+#endif
 #pragma unroll
         for (int mt = 0; mt < 2; mt++) {
+#if SEM_MLP_LDSM
+            ldsm_x4(a[mt], xs + (wr + mt * 16 + a_row) * KP1 + ks * 16 + a_col);
+#else
             const int r = wr + mt * 16 + g;
             a[mt][0] = *reinterpret_cast<const uint32_t *>(xs + r * KP1 + k0);
             a[mt][1] = *reinterpret_cast<const uint32_t *>(xs + (r + 8) * KP1 + k0);
             a[mt][2] = *reinterpret_cast<const uint32_t *>(xs + r * KP1 + k0 + 8);
             a[mt][3] = *reinterpret_cast<const uint32_t *>(xs + (r + 8) * KP1 + k0 + 8);
+#endif
         }
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
+#if SEM_MLP_LDSM
+            uint32_t b[2];
+            ldsm_x2(b, s.w1 + (nt * 8 + b_row) * KP1 + ks * 16 + b_col);
+#else
             const int n = nt * 8 + g;
             const uint32_t b[2] = {*reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0),
                                    *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0 + 8)};
+#endif
             mma16816(acc[0][nt], a[0], b);
             mma16816(acc[1][nt], a[1], b);
         }
@@ -278,12 +327,19 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
         }
 #pragma unroll
     for (int ks = 0; ks < H / 16; ks++) {
+#if !SEM_MLP_LDSM
         const int k0 = ks * 16 + q * 2;
+#endif
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
+#if SEM_MLP_LDSM
+            uint32_t b[2];
+            ldsm_x2(b, s.w2 + (nt * 8 + b_row) * KP2 + ks * 16 + b_col);
+#else
             const int n = nt * 8 + g;
             const uint32_t b[2] = {*reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0),
                                    *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0 + 8)};
+#endif
             mma16816(acc[0][nt], h[0][ks], b);
             mma16816(acc[1][nt], h[1][ks], b);
         }
@@ -682,11 +738,13 @@ __global__ void __launch_bounds__(128, 4) k_abc_correction(const MlpDev net, con
 
 constexpr int kPU = kFaceTU + 2, kPV = kFaceTV + 2, kPD = kPU * kPV;  // patch plane with its rim
 constexpr int kPL = 3 * kPD;  // one level: depth planes outside (zeros), face, inside
-// shared layout after the weights: xs, scale, then the patch [3 levels][3 depths][kPV][kPU] and
-// the 27 neighbour offsets
+// shared layout after the weights: xs, scale, then the patch [3 levels][3 depths][kPV][kPU],
+// each row's output node (-1: none) and the 27 neighbour offsets
 constexpr size_t kFaceXsOff = kAbcXsOff;
 constexpr size_t kFacePatchOff = kFaceXsOff + sizeof(uint16_t) * T * KP1 + sizeof(float) * T;
-constexpr size_t kFaceOffsOff = kFacePatchOff + sizeof(float) * 3 * kPL;
+constexpr size_t kFaceOutOff = kFacePatchOff + sizeof(float) * 3 * kPL;
+constexpr size_t kFaceOffsOff = kFaceOutOff + sizeof(int64_t) * T;
+static_assert(kFaceOutOff % 8 == 0, "8-byte aligned output nodes");
 
 __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const AbcFaceArgs a)
 {
@@ -695,55 +753,47 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
     uint16_t *xs = reinterpret_cast<uint16_t *>(smem + kFaceXsOff);
     float *scale = reinterpret_cast<float *>(xs + T * KP1);
     float *patch = reinterpret_cast<float *>(smem + kFacePatchOff);
+    int64_t *onode = reinterpret_cast<int64_t *>(smem + kFaceOutOff);
     int *offs = reinterpret_cast<int *>(smem + kFaceOffsOff);
     load_net(s, net);
     // the depth plane outside the box stays zero for every tile
     for (int i = threadIdx.x; i < 3 * kPD; i += blockDim.x) patch[(i / kPD) * kPL + i % kPD] = 0.f;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
     const int64_t plane = a.nxp * a.nz;
-    for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        __syncthreads();  // the previous tile's patch, offsets and rows are consumed
-        const int4 td = a.tiles[t];
-        const FaceDesc f = a.face[td.x];
-        const int u0 = td.y, v0 = td.z;
-        if (threadIdx.x < 27) {
-            // feature neighbour nb = (dz+1)*9 + (dy+1)*3 + (dx+1) -> offset within a level's patch
-            const int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
-            auto along = [&](int axis) { return axis == 0 ? dx : (axis == 1 ? dy : dz); };
-            offs[threadIdx.x] = along(f.axis_n) * f.inward * kPD + along(f.axis_v) * kPU + along(f.axis_u);
+    // A tile stages the face and inside planes of the three levels with a one-node rim: a thread
+    // takes a position (depth, v, u) and loads it from all three levels, sharing the index
+    // arithmetic and the node's sponge factor.  x-faces step through the depth fastest (adjacent
+    // in memory), the others along u (rows along x).
+    constexpr int NPOS = 2 * kPD, KS = (NPOS + T - 1) / T;
+    // position i of the patch: depth (1: face, 2: inside), position along v and u
+    auto decode = [&](const FaceDesc &f, int i, int &di, int &vv, int &uu) {
+        if (f.axis_n == 0) {
+            di = i % 2 + 1;
+            const int r = i / 2;
+            uu = r % kPU; vv = r / kPU;
+        } else {
+            uu = i % kPU;
+            const int r = i / kPU;
+            vv = r % kPV; di = r / kPV + 1;
         }
-        // stage the face and inside planes of the three levels with a one-node rim: a thread takes
-        // a position (depth, v, u) and loads it from all three levels, sharing the index
-        // arithmetic and the node's sponge factor.  x-faces step through the depth fastest
-        // (adjacent in memory), the others along u (rows along x).  All of a thread's loads are
-        // issued first (one round trip), then stored.
-        const bool depth_fast = f.axis_n == 0;
-        constexpr int NPOS = 2 * kPD, KS = (NPOS + T - 1) / T;
-        // position i of the patch: depth (1: face, 2: inside), position along v and u
-        auto decode = [&](int i, int &di, int &vv, int &uu) {
-            if (depth_fast) {
-                di = i % 2 + 1;
-                const int r = i / 2;
-                uu = r % kPU; vv = r / kPU;
-            } else {
-                uu = i % kPU;
-                const int r = i / kPU;
-                vv = r % kPV; di = r / kPV + 1;
-            }
-        };
-        // node coordinates by axis (selects, not an indexed array: they stay in registers)
-        auto coords = [&](int di, int vv, int uu, int &cx, int &cy, int &cz) {
-            const int cu = u0 - 1 + uu, cv = v0 - 1 + vv, cn = f.side + (di - 1) * f.inward;
-            cx = f.axis_u == 0 ? cu : (f.axis_v == 0 ? cv : cn);
-            cy = f.axis_u == 1 ? cu : (f.axis_v == 1 ? cv : cn);
-            cz = f.axis_u == 2 ? cu : (f.axis_v == 2 ? cv : cn);
-        };
-        // p^{n+1} of a boundary node is the stored p^{n-1} twice damped (the step keeps the
-        // Dirichlet value): s * (s * p^{n-1}) = s * hist, the same bits, so boundary nodes take
-        // level 0 from the history and this kernel can write their new values in place (no tile
-        // reads p^{n+1} of a boundary node).  s = (sx*sz)*sy, as the step rounds it.
-        float v0s[KS], v1s[KS], v2s[KS], sfs[KS];
-        bool bnds[KS];
+    };
+    // node coordinates by axis (selects, not an indexed array: they stay in registers)
+    auto coords = [&](const FaceDesc &f, int u0, int v0, int di, int vv, int uu, int &cx, int &cy, int &cz) {
+        const int cu = u0 - 1 + uu, cv = v0 - 1 + vv, cn = f.side + (di - 1) * f.inward;
+        cx = f.axis_u == 0 ? cu : (f.axis_v == 0 ? cv : cn);
+        cy = f.axis_u == 1 ? cu : (f.axis_v == 1 ? cv : cn);
+        cz = f.axis_u == 2 ? cu : (f.axis_v == 2 ? cv : cn);
+    };
+    // p^{n+1} of a boundary node is the stored p^{n-1} twice damped (the step keeps the
+    // Dirichlet value): s * (s * p^{n-1}) = s * hist, the same bits, so boundary nodes take
+    // level 0 from the history and this kernel can write their new values in place (no tile
+    // reads p^{n+1} of a boundary node, so a tile's loads may run ahead of other tiles' writes).
+    // s = (sx*sz)*sy, as the step rounds it.
+    float v0s[KS], v1s[KS], v2s[KS], sfs[KS];
+    bool bnds[KS];
+    auto load_patch = [&](int64_t tt) {
+        const int4 td = a.tiles[tt];
+        const FaceDesc f = a.face[td.x];
 #pragma unroll
         for (int k = 0; k < KS; k++) {
             const int i = threadIdx.x + k * T;
@@ -752,8 +802,8 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
             bnds[k] = false;
             if (i < NPOS) {
                 int di, vv, uu, cx, cy, cz;
-                decode(i, di, vv, uu);
-                coords(di, vv, uu, cx, cy, cz);
+                decode(f, i, di, vv, uu);
+                coords(f, td.y, td.z, di, vv, uu, cx, cy, cz);
                 if (cx >= 0 && cx < a.nx && cy >= 0 && cy < a.ny && cz >= 0 && cz < a.nz) {
                     const int64_t qn = cx + (int64_t)cz * a.nxp + (int64_t)cy * plane;
                     bnds[k] = cx == 0 || cx == a.nx - 1 || cy == 0 || cy == a.ny - 1 || cz == 0 || cz == a.nz - 1;
@@ -764,20 +814,30 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
                 }
             }
         }
+    };
+    auto store_patch = [&](int64_t tt) {
+        const int4 td = a.tiles[tt];
+        const FaceDesc f = a.face[td.x];
+        if (threadIdx.x < 27) {
+            // feature neighbour nb = (dz+1)*9 + (dy+1)*3 + (dx+1) -> offset within a level's patch
+            const int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
+            auto along = [&](int axis) { return axis == 0 ? dx : (axis == 1 ? dy : dz); };
+            offs[threadIdx.x] = along(f.axis_n) * f.inward * kPD + along(f.axis_v) * kPU + along(f.axis_u);
+        }
 #pragma unroll
         for (int k = 0; k < KS; k++) {
             const int i = threadIdx.x + k * T;
             if (i < NPOS) {
                 int di, vv, uu;
-                decode(i, di, vv, uu);
+                decode(f, i, di, vv, uu);
                 const float p0 = bnds[k] ? v2s[k] * sfs[k] : v0s[k];
                 const float p1 = v1s[k] * sfs[k];  // p^n is stored without its last sponge factor
                 // p^n of the tile's own nodes and their inside neighbours: the next step's
                 // p^{n-1} (every node of the two-node shell is one of these for some tile)
-                const int us = u0 - 1 + uu, vs = v0 - 1 + vv;
+                const int us = td.y - 1 + uu, vs = td.z - 1 + vv;
                 if (uu >= 1 && uu <= kFaceTU && vv >= 1 && vv <= kFaceTV && us < f.uhi && vs < f.vhi) {
                     int cx, cy, cz;
-                    coords(di, vv, uu, cx, cy, cz);
+                    coords(f, td.y, td.z, di, vv, uu, cx, cy, cz);
                     a.hist_next[cx + (int64_t)cz * a.nxp + (int64_t)cy * plane] = p1;
                 }
                 const int o = di * kPD + vv * kPU + uu;
@@ -786,13 +846,33 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
                 patch[2 * kPL + o] = v2s[k];
             }
         }
+    };
+#if SEM_MLP_FACE_PIPE
+    if (blockIdx.x < a.ntiles) {
+        load_patch(blockIdx.x);
+        store_patch(blockIdx.x);
+    }
+#endif
+    for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+#if SEM_MLP_FACE_PIPE
+        __syncthreads();  // tile t's patch and offsets are staged
+#else
+        __syncthreads();  // the previous tile's patch, offsets and rows are consumed
+        load_patch(t);
+        store_patch(t);
         __syncthreads();
+#endif
         // features of the row's node from the patch (as k_abc_correction gathers them)
         const int r = threadIdx.x;
+        const int4 td = a.tiles[t];
         const int64_t pos = a.pos[t * T + r];
         const int base = kPD + (r / kFaceTU + 1) * kPU + (r % kFaceTU + 1);
         uint16_t *xr = xs + r * KP1;
         if (pos >= 0) {
+            // the row's node on the face plane, where the network's output goes
+            int cx, cy, cz;
+            coords(a.face[td.x], td.y, td.z, 1, r / kFaceTU + 1, r % kFaceTU + 1, cx, cy, cz);
+            onode[r] = cx + (int64_t)cz * a.nxp + (int64_t)cy * plane;
             float v[3][27];
 #pragma unroll
             for (int l = 0; l < 3; l++)
@@ -821,10 +901,16 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
             for (int c = 0; c < kMlpInPad / 8; c++)
                 reinterpret_cast<uint4 *>(xr)[c] = make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
         } else {
+            onode[r] = -1;
             scale[r] = 1e-30f;
 #pragma unroll
             for (int c = 0; c < kMlpInPad / 8; c++) reinterpret_cast<uint4 *>(xr)[c] = make_uint4(0, 0, 0, 0);
         }
+#if SEM_MLP_FACE_PIPE
+        // the next tile's loads are in flight while this tile runs the network
+        const int64_t tn = t + gridDim.x;
+        if (tn < a.ntiles) load_patch(tn);
+#endif
         __syncwarp();
         float yv[2][2];
         forward_rows_regs(s, xs, w * 32, yv);
@@ -833,14 +919,15 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
             for (int mt = 0; mt < 2; mt++)
 #pragma unroll
                 for (int hrow = 0; hrow < 2; hrow++) {
+                    // rows of this warp: their nodes and scales were written by its own lanes
                     const int rr = w * 32 + mt * 16 + g + hrow * 8;
-                    if (a.pos[t * T + rr] >= 0) {
-                        int cx, cy, cz;
-                        coords(1, rr / kFaceTU + 1, rr % kFaceTU + 1, cx, cy, cz);
-                        a.p_new[cx + (int64_t)cz * a.nxp + (int64_t)cy * plane] =
-                            scale[rr] * fminf(fmaxf(yv[mt][hrow], -1.f), 1.f);
-                    }
+                    const int64_t o = onode[rr];
+                    if (o >= 0) a.p_new[o] = scale[rr] * fminf(fmaxf(yv[mt][hrow], -1.f), 1.f);
                 }
+#if SEM_MLP_FACE_PIPE
+        __syncthreads();  // every warp has read tile t's patch and offsets
+        if (tn < a.ntiles) store_patch(tn);
+#endif
     }
 }
 
