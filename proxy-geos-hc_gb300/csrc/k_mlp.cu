@@ -856,7 +856,9 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
     // level 0 from the history and this kernel can write their new values in place (no tile
     // reads p^{n+1} of a boundary node, so a tile's loads may run ahead of other tiles' writes).
     // s = (sx*sz)*sy, as the step rounds it.
-    float v0s[KS], v1s[KS], v2s[KS], sfs[KS];
+    // the three sponge factors are kept apart until the store, so that no arithmetic waits on the
+    // loads before the network runs
+    float v0s[KS], v1s[KS], v2s[KS], sxs[KS], sys[KS], szs[KS];
     bool bnds[KS];
     auto load_patch = [&](int64_t tt) {
         const int4 td = a.tiles[tt];
@@ -865,7 +867,7 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
         for (int k = 0; k < KS; k++) {
             const int i = threadIdx.x + k * T;
             v0s[k] = v1s[k] = v2s[k] = 0.f;
-            sfs[k] = 1.f;
+            sxs[k] = sys[k] = szs[k] = 1.f;
             bnds[k] = false;
             if (i < NPOS) {
                 int di, vv, uu, cx, cy, cz;
@@ -877,11 +879,16 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
                     v2s[k] = a.hist[qn];
                     v1s[k] = a.p_cur[qn];
                     if (!bnds[k]) v0s[k] = a.p_new[qn];
-                    if (a.sx) sfs[k] = (__ldg(a.sx + cx) * __ldg(a.sz + cz)) * __ldg(a.sy + cy);
+                    if (a.sx) {
+                        sxs[k] = __ldg(a.sx + cx);
+                        sys[k] = __ldg(a.sy + cy);
+                        szs[k] = __ldg(a.sz + cz);
+                    }
                 }
             }
         }
     };
+    // returns the tile's descriptor
     auto store_patch = [&](int64_t tt) {
         const int4 td = a.tiles[tt];
         const FaceDesc f = a.face[td.x];
@@ -897,8 +904,9 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
             if (i < NPOS) {
                 int di, vv, uu;
                 decode(f, i, di, vv, uu);
-                const float p0 = bnds[k] ? v2s[k] * sfs[k] : v0s[k];
-                const float p1 = v1s[k] * sfs[k];  // p^n is stored without its last sponge factor
+                const float sf = (sxs[k] * szs[k]) * sys[k];
+                const float p0 = bnds[k] ? v2s[k] * sf : v0s[k];
+                const float p1 = v1s[k] * sf;  // p^n is stored without its last sponge factor
                 // p^n of the tile's own nodes and their inside neighbours: the next step's
                 // p^{n-1} (every node of the two-node shell is one of these for some tile)
                 const int us = td.y - 1 + uu, vs = td.z - 1 + vv;
@@ -913,11 +921,13 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
                 patch[2 * kPL + o] = v2s[k];
             }
         }
+        return td;
     };
+    int4 td = make_int4(0, 0, 0, 0);  // the current tile's descriptor
 #if SEM_MLP_FACE_PIPE
     if (blockIdx.x < a.ntiles) {
         load_patch(blockIdx.x);
-        store_patch(blockIdx.x);
+        td = store_patch(blockIdx.x);
     }
 #endif
     for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
@@ -926,30 +936,37 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
 #else
         __syncthreads();  // the previous tile's patch, offsets and rows are consumed
         load_patch(t);
-        store_patch(t);
+        td = store_patch(t);
         __syncthreads();
 #endif
-        // features of the row's node from the patch (as k_abc_correction gathers them)
+        // features of the row's node from the patch (as k_abc_correction gathers them).  The
+        // row's node is on the face if it lies within the face's ranges (every such node is a
+        // boundary node, so this is the tile's strip position being valid).
         const int r = threadIdx.x;
-        const int4 td = a.tiles[t];
-        const int64_t pos = a.pos[t * T + r];
+        const FaceDesc &fc = a.face[td.x];
+        const bool valid = td.y + r % kFaceTU < fc.uhi && td.z + r / kFaceTU < fc.vhi;
         const int base = kPD + (r / kFaceTU + 1) * kPU + (r % kFaceTU + 1);
         uint16_t *xr = xs + r * KP1;
-        if (pos >= 0) {
+        if (valid) {
             // the row's node on the face plane, where the network's output goes
             int cx, cy, cz;
-            coords(a.face[td.x], td.y, td.z, 1, r / kFaceTU + 1, r % kFaceTU + 1, cx, cy, cz);
+            coords(fc, td.y, td.z, 1, r / kFaceTU + 1, r % kFaceTU + 1, cx, cy, cz);
             onode[r] = cx + (int64_t)cz * a.nxp + (int64_t)cy * plane;
             float v[3][27];
 #pragma unroll
             for (int l = 0; l < 3; l++)
 #pragma unroll
                 for (int nb = 0; nb < 27; nb++) v[l][nb] = patch[l * kPL + base + offs[nb]];
-            float m = 0.f;
+            // the largest magnitude in nine independent chains (the same value in any order)
+            float mm[9];
+#pragma unroll
+            for (int j = 0; j < 9; j++) mm[j] = 0.f;
 #pragma unroll
             for (int l = 0; l < 3; l++)
 #pragma unroll
-                for (int nb = 0; nb < 27; nb++) m = fmaxf(m, fabsf(v[l][nb]));
+                for (int nb = 0; nb < 27; nb++) mm[nb % 9] = fmaxf(mm[nb % 9], fabsf(v[l][nb]));
+            const float m = fmaxf(fmaxf(fmaxf(mm[0], mm[1]), fmaxf(mm[2], mm[3])),
+                                  fmaxf(fmaxf(mm[4], mm[5]), fmaxf(fmaxf(mm[6], mm[7]), mm[8])));
             const float sc = m + 1e-30f;
             scale[r] = sc;
             const float inv = 1.f / sc;
@@ -993,7 +1010,7 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
                 }
 #if SEM_MLP_FACE_PIPE
         __syncthreads();  // every warp has read tile t's patch and offsets
-        if (tn < a.ntiles) store_patch(tn);
+        if (tn < a.ntiles) td = store_patch(tn);
 #endif
     }
 }
