@@ -68,6 +68,16 @@ enum { SEM_FORM_DIRECT = 0, SEM_FORM_DIFFERENCE = 1 };
    DEFAULT. */
 enum { SEM_ROUNDING_DEFAULT = 0, SEM_ROUNDING_REFERENCE = 1 };
 
+/* Tile shape of the stencil pass (sem_solver_set_tile_shape): the nodes along x and z that one
+   CTA steps.  DEFAULT: 16o x 8 for o = 1, 2 and 4 (64 x 16 at order 4), 48 x 24 at o = 3, 40 x 20
+   at o = 5.  SQUARE: 32 x 32 at order 4 (other orders: the default), for the plain step of one
+   shot in the default rounding (the reference rounding, the adjoint's passes, batches and the
+   one-launch group form keep the default).  AUTO: the shape whose busiest CTA slot marches the
+   fewest planes per lane on a node, from the box's node counts (on GB300, 345^3 and 401^3 nodes
+   take the square tile: 0.130 against 0.145 ms and 336 against 322 Gnode-steps/s; 481^3 and
+   801^3 keep the default).  Every shape gives the same bits. */
+enum { SEM_TILE_AUTO = -1, SEM_TILE_DEFAULT = 0, SEM_TILE_SQUARE = 1 };
+
 /* Pressure levels for sem_solver_get_pressure / sem_solver_set_pressure. */
 enum { SEM_LEVEL_CURRENT = 0, SEM_LEVEL_PREVIOUS = 1 };
 
@@ -196,6 +206,13 @@ int sem_solver_set_operator_form(sem_solver *s, int form);
    bit for bit where its float node coordinates are exact (orders 1 and 2 with integer element
    sizes).  SEM_ROUNDING_REFERENCE ignores the operator form.  Extension: parity mode. */
 int sem_solver_set_rounding(sem_solver *s, int rounding);
+
+/* Tile shape of the stencil pass (SEM_TILE_*; default SEM_TILE_AUTO).  Extension. */
+int sem_solver_set_tile_shape(sem_solver *s, int shape);
+
+/* The shape the solver's stencil tables were built with (SEM_TILE_DEFAULT or SEM_TILE_SQUARE);
+   SEM_TILE_AUTO before the first stencil step builds them. */
+int sem_solver_get_tile_shape(const sem_solver *s, int *shape);
 
 /* Sponge of `thickness` elements with boundary damping sigma (0 thickness: none), or explicit
  * per-axis factors (see sem_box_sponge_profile).  Applied after each step to both levels. */

@@ -154,6 +154,11 @@ int sem_adjoint_create(sem_mesh *m, float dt, int n_steps, int checkpoint_every,
     if (rc == SEM_OK) rc = sem_solver_set_kernel(a->fwd, SEM_KERNEL_STENCIL);
     if (rc == SEM_OK) rc = sem_solver_set_kernel(a->adj, SEM_KERNEL_STENCIL);
     if (rc == SEM_OK) rc = sem_solver_set_stream(a->adj, a->fwd->stream);
+    if (rc == SEM_OK) {
+        // the recording and gradient passes are built for the default tile shape
+        a->fwd->tile_shape = semgb::kTileDefault;
+        a->adj->tile_shape = semgb::kTileDefault;
+    }
     if (rc != SEM_OK) {
         sem_adjoint_destroy(a);
         return rc;

@@ -596,6 +596,28 @@ int sem_solver_set_rounding(sem_solver *s, int rounding)
     return SEM_OK;
 }
 
+int sem_solver_set_tile_shape(sem_solver *s, int shape)
+{
+    if (!s) return fail(SEM_ERR_ARG, "NULL solver");
+    if (shape != SEM_TILE_AUTO && shape != SEM_TILE_DEFAULT && shape != SEM_TILE_SQUARE)
+        return fail(SEM_ERR_ARG, "unknown tile shape");
+    static_assert(SEM_TILE_DEFAULT == kTileDefault && SEM_TILE_SQUARE == kTileSquare, "tile shapes");
+    if (shape != s->tile_shape) {
+        cudaStreamSynchronize(s->stream);
+        solver_invalidate_graphs(s);
+        stencil_tables_free(s->stencil);  // rebuilt by the next step
+        s->tile_shape = shape;
+    }
+    return SEM_OK;
+}
+
+int sem_solver_get_tile_shape(const sem_solver *s, int *shape)
+{
+    if (!s || !shape) return fail(SEM_ERR_ARG, "NULL argument");
+    *shape = s->stencil ? s->stencil->shape : SEM_TILE_AUTO;
+    return SEM_OK;
+}
+
 int sem_solver_set_sponge_profile(sem_solver *s, const float *sx, const float *sy, const float *sz)
 {
     GUARD_BEGIN
@@ -772,11 +794,17 @@ int solver_prepare(sem_solver *s, int64_t n_new)
             solver_invalidate_graphs(s);
         }
     } else {
+        const bool want_class = s->rounding == SEM_ROUNDING_REFERENCE;
+        // the reference rounding runs on the default tile shape
+        const int shape = want_class ? kTileDefault : s->tile_shape;
+        if (s->stencil && shape == kTileDefault && s->stencil->shape != kTileDefault) {
+            stencil_tables_free(s->stencil);
+            solver_invalidate_graphs(s);
+        }
         if (!s->stencil) {
-            int rc = stencil_tables_create(m->box, m->gll, m->geo, 1, &s->stencil);
+            int rc = stencil_tables_create(m->box, m->gll, m->geo, 1, &s->stencil, shape);
             if (rc) return fail(SEM_ERR_CUDA, "stencil tables");
         }
-        const bool want_class = s->rounding == SEM_ROUNDING_REFERENCE;
         if (want_class != (s->stencil->class_tab != nullptr)) {
             std::vector<float> tab;
             const Box &b = m->box;

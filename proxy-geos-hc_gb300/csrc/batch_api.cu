@@ -195,7 +195,7 @@ int sem_batch_create(sem_mesh *m, float dt, int n_shots, sem_batch **out)
         (e = cudaMemcpy(b->d_w, m->gll.w, (m->box.order + 1) * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
         return cleanup(SEM_ERR_CUDA, cudaGetErrorString(e));
     if ((e = stencil_kernel_setup()) != cudaSuccess) return cleanup(SEM_ERR_CUDA, std::string("kernel set-up: ") + cudaGetErrorString(e));
-    if (stencil_tables_create(m->box, m->gll, m->geo, n_shots, &b->st) != 0) return cleanup(SEM_ERR_CUDA, "stencil tables");
+    if (stencil_tables_create(m->box, m->gll, m->geo, n_shots, &b->st, kTileDefault) != 0) return cleanup(SEM_ERR_CUDA, "stencil tables");
     b->tune.warps_per_cta = b->st->threads / 32;
     b->tune.ychunk = b->st->ychunk;
     *out = b;

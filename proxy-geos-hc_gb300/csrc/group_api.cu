@@ -150,7 +150,9 @@ std::vector<int> group_chunks(const sem_group *g, int64_t resident)
         jobs.clear();
         for (const sem_solver *s : g->members) {
             const Box &b = s->mesh->box;
-            const int64_t cols = (int64_t)s->stencil->grid[0] * s->stencil->grid[1];
+            int tx = 0, tz = 0, hx = 0, th = 0;  // the group's tiles have the default shape
+            semgb::stencil_tile_dims(b.order, semgb::kTileDefault, tx, tz, hx, th);
+            const int64_t cols = ((b.nx + tx - 1) / tx) * ((b.nz + tz - 1) / tz);
             const int64_t c = (b.ny + L - 1) / L, chunk = (b.ny + c - 1) / c;
             jobs.push_back({chunk + 2 * b.order, cols * c});
         }
@@ -257,13 +259,16 @@ int build_one_launch(sem_group *g)
     if (g->ones.size() != n) g->ones.assign(n, nullptr);
     for (size_t i = 0; i < n; i++) {
         sem_solver *s = g->members[i];
-        StencilTables *t = new StencilTables(*s->stencil);  // tensor maps of the member's levels
-        t->class_tab = nullptr;
-        t->d_rec_off = nullptr;
-        t->d_rec_idx = nullptr;
+        // tables of the default tile shape (the group kernel's) over the member's levels: a
+        // member stepped alone may use another shape
+        StencilTables *t = nullptr;
+        if (semgb::stencil_tables_create(s->mesh->box, s->mesh->gll, s->mesh->geo, 1, &t, semgb::kTileDefault) != 0)
+            return sem_fail(SEM_ERR_CUDA, "stencil tables");
+        g->tabs[i] = t;
+        if (semgb::stencil_bind(*t, s->d_p[0], s->d_p[1], s->d_a) != 0)
+            return sem_fail(SEM_ERR_CUDA, "tensor-map encoding failed (driver entry point cuTensorMapEncodeTiled)");
         t->ychunk = chunks[i];
         t->grid[2] = (int)((t->ny + chunks[i] - 1) / chunks[i]);
-        g->tabs[i] = t;
         CUDA_TRY(semgb::stencil_set_receivers(*t, s->rec_sorted.data(), s->nrec, s->rec_version));
         if (!s->sponge && !g->ones[i]) {
             const Box &b = s->mesh->box;

@@ -32,8 +32,8 @@ namespace semgb {
 
 namespace {
 
-template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF = false>
-__global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF = false, int RWS = SEM_STENCIL_RW>
+__global__ void __launch_bounds__(Cfg<O, RWS>::THREADS, Cfg<O, RWS>::MIN_BLOCKS)
     k_stencil(const __grid_constant__ CUtensorMap ring_map, const __grid_constant__ CUtensorMap win_map,
               const __grid_constant__ CUtensorMap prev_map, const __grid_constant__ CUtensorMap a_map,
               const StencilTables t, const StencilArgs a, const __grid_constant__ ClassParam<O, REF> ct)
@@ -54,69 +54,59 @@ __global__ void __launch_bounds__(Cfg<O>::THREADS, Cfg<O>::MIN_BLOCKS)
         bz = (int)blockIdx.y;
         chunk = (int)blockIdx.z;
     }
-    stencil_cta<O, SPONGE, MODE, DIRECT, MULTI, REF, false>(&ring_map, &win_map, &prev_map, &a_map, t, a, ct, shot, bx,
-                                                            bz, chunk);
+    stencil_cta<O, SPONGE, MODE, DIRECT, MULTI, REF, false, RWS>(&ring_map, &win_map, &prev_map, &a_map, t, a, ct,
+                                                                 shot, bx, bz, chunk);
 }
 
-template <int O>
-size_t smem_of() { return Cfg<O>::SMEM; }
+template <int O, int RWS = SEM_STENCIL_RW>
+size_t smem_of() { return Cfg<O, RWS>::SMEM; }
 
-size_t smem_bytes(int order)
+size_t smem_bytes(int order, int shape)
 {
     switch (order) {
     case 1: return smem_of<1>();
     case 2: return smem_of<2>();
     case 3: return smem_of<3>();
-    case 4: return smem_of<4>();
+    case 4: return shape == kTileSquare ? smem_of<4, kSquareRW>() : smem_of<4>();
     default: return smem_of<5>();
     }
 }
 
-template <int O>
+template <int O, int RWS = SEM_STENCIL_RW>
 void tile_of(int &tx, int &tz, int &hx, int &th)
 {
-    tx = Cfg<O>::TX; tz = Cfg<O>::TZ; hx = Cfg<O>::HX; th = Cfg<O>::THREADS;
-}
-
-void tile_dims(int order, int &tx, int &tz, int &hx, int &th)
-{
-    switch (order) {
-    case 1: tile_of<1>(tx, tz, hx, th); break;
-    case 2: tile_of<2>(tx, tz, hx, th); break;
-    case 3: tile_of<3>(tx, tz, hx, th); break;
-    case 4: tile_of<4>(tx, tz, hx, th); break;
-    default: tile_of<5>(tx, tz, hx, th); break;
-    }
+    tx = Cfg<O, RWS>::TX; tz = Cfg<O, RWS>::TZ; hx = Cfg<O, RWS>::HX; th = Cfg<O, RWS>::THREADS;
 }
 
 // resident CTAs per SM of the sponge variant (the others use no more registers); 0 if unknown
-template <int O>
+template <int O, int RWS = SEM_STENCIL_RW>
 int blocks_per_sm_of()
 {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stencil<O, true, STENCIL_PLAIN, true, false>, Cfg<O>::THREADS,
-                                                      Cfg<O>::SMEM) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_stencil<O, true, STENCIL_PLAIN, true, false, false, RWS>,
+                                                      Cfg<O, RWS>::THREADS, Cfg<O, RWS>::SMEM) != cudaSuccess) {
         cudaGetLastError();
         n = 0;
     }
     return n;
 }
 
-int blocks_per_sm(int order)
+int blocks_per_sm(int order, int shape)
 {
     switch (order) {
     case 1: return blocks_per_sm_of<1>();
     case 2: return blocks_per_sm_of<2>();
     case 3: return blocks_per_sm_of<3>();
-    case 4: return blocks_per_sm_of<4>();
+    case 4: return shape == kTileSquare ? blocks_per_sm_of<4, kSquareRW>() : blocks_per_sm_of<4>();
     default: return blocks_per_sm_of<5>();
     }
 }
 
-template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF = false>
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF = false, int RWS = SEM_STENCIL_RW>
 void launch_om(const dim3 &grid, const LevelMaps &cm, const LevelMaps &pm, const StencilTables &t,
                const StencilArgs &a, cudaStream_t s)
 {
+    using C = Cfg<O, RWS>;
     ClassParam<O, REF> ct{};
     if constexpr (REF) std::memcpy(ct.c, t.class_tab, sizeof ct.c);
     if (MULTI && t.cluster > 1) {
@@ -125,8 +115,8 @@ void launch_om(const dim3 &grid, const LevelMaps &cm, const LevelMaps &pm, const
         // still in L2 when the later ones read it
         cudaLaunchConfig_t cfg{};
         cfg.gridDim = grid;
-        cfg.blockDim = dim3(Cfg<O>::THREADS);
-        cfg.dynamicSmemBytes = Cfg<O>::SMEM;
+        cfg.blockDim = dim3(C::THREADS);
+        cfg.dynamicSmemBytes = C::SMEM;
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -139,14 +129,25 @@ void launch_om(const dim3 &grid, const LevelMaps &cm, const LevelMaps &pm, const
                            a, ct);
         return;
     }
-    k_stencil<O, SPONGE, MODE, DIRECT, MULTI, REF>
-        <<<grid, Cfg<O>::THREADS, Cfg<O>::SMEM, s>>>(cm.tile, cm.win, pm.tile, t.amap, t, a, ct);
+    k_stencil<O, SPONGE, MODE, DIRECT, MULTI, REF, RWS>
+        <<<grid, C::THREADS, C::SMEM, s>>>(cm.tile, cm.win, pm.tile, t.amap, t, a, ct);
 }
 
 template <int O, bool DIRECT>
 cudaError_t launch_of(const StencilTables &t, const StencilArgs &a, int ci, bool sponge, int mode, cudaStream_t s)
 {
     const LevelMaps &cm = t.lv[ci], &pm = t.lv[1 - ci];
+    if (t.shape == kTileSquare) {
+        // the square order-4 tile: single-shot plain steps in the tensor-product operator
+        if constexpr (O == 4) {
+            if (t.class_tab || t.nshot != 1 || mode != STENCIL_PLAIN) return cudaErrorInvalidValue;
+            const dim3 grid(t.grid[0], t.grid[1], t.grid[2]);
+            if (sponge) launch_om<O, true, STENCIL_PLAIN, DIRECT, false, false, kSquareRW>(grid, cm, pm, t, a, s);
+            else launch_om<O, false, STENCIL_PLAIN, DIRECT, false, false, kSquareRW>(grid, cm, pm, t, a, s);
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
+    }
     if (t.class_tab) {
         // reference rounding: plain steps with the node-class table (one shot or many)
         if constexpr (DIRECT) {
@@ -195,11 +196,11 @@ cudaError_t launch_o(const StencilTables &t, const StencilArgs &a, int ci, bool 
     return direct ? launch_of<O, true>(t, a, ci, sponge, mode, s) : launch_of<O, false>(t, a, ci, sponge, mode, s);
 }
 
-template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI = false, bool REF = false>
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI = false, bool REF = false, int RWS = SEM_STENCIL_RW>
 cudaError_t setup_om()
 {
-    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE, DIRECT, MULTI, REF>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<O>::SMEM);
+    return cudaFuncSetAttribute(k_stencil<O, SPONGE, MODE, DIRECT, MULTI, REF, RWS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<O, RWS>::SMEM);
 }
 
 template <int O, bool DIRECT>
@@ -225,6 +226,12 @@ cudaError_t setup_o()
     if (e == cudaSuccess) e = setup_om<O, false, STENCIL_PLAIN, true, false, true>();
     if (e == cudaSuccess) e = setup_om<O, true, STENCIL_PLAIN, true, true, true>();
     if (e == cudaSuccess) e = setup_om<O, false, STENCIL_PLAIN, true, true, true>();
+    if constexpr (O == 4) {
+        if (e == cudaSuccess) e = setup_om<O, true, STENCIL_PLAIN, true, false, false, kSquareRW>();
+        if (e == cudaSuccess) e = setup_om<O, false, STENCIL_PLAIN, true, false, false, kSquareRW>();
+        if (e == cudaSuccess) e = setup_om<O, true, STENCIL_PLAIN, false, false, false, kSquareRW>();
+        if (e == cudaSuccess) e = setup_om<O, false, STENCIL_PLAIN, false, false, false, kSquareRW>();
+    }
     return e;
 }
 
@@ -237,7 +244,21 @@ bool make_map(CUtensorMap &m, const float *base, const StencilTables &t, int bx,
 
 }  // namespace
 
-int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int nshot, StencilTables **out)
+void stencil_tile_dims(int order, int shape, int &tx, int &tz, int &hx, int &threads)
+{
+    switch (order) {
+    case 1: tile_of<1>(tx, tz, hx, threads); break;
+    case 2: tile_of<2>(tx, tz, hx, threads); break;
+    case 3: tile_of<3>(tx, tz, hx, threads); break;
+    case 4:
+        if (shape == kTileSquare) tile_of<4, kSquareRW>(tx, tz, hx, threads);
+        else tile_of<4>(tx, tz, hx, threads);
+        break;
+    default: tile_of<5>(tx, tz, hx, threads); break;
+    }
+}
+
+int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int nshot, StencilTables **out, int shape)
 {
     if (nshot < 1) return (int)cudaErrorInvalidValue;
     StencilTables *t = new StencilTables();
@@ -247,30 +268,53 @@ int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int n
     t->shot_stride = b.nxp * b.nz * b.ny;
     for (int d = 0; d < 3; d++) t->g[d] = (float)geo.g[d];
     for (int l = 0; l < b.order; l++) t->wa[l] = (float)(l == 0 ? g.w[0] + g.w[b.order] : g.w[l]);
-    int threads = 256;
-    tile_dims(b.order, t->tile_x, t->tile_z, t->halo_x, threads);
-    t->threads = threads;
-    t->smem = smem_bytes(b.order);
-    t->grid[0] = (int)((b.nx + t->tile_x - 1) / t->tile_x);
-    t->grid[1] = (int)((b.nz + t->tile_z - 1) / t->tile_z);
-    // y-chunking: balance the last wave against the 2o warm-up planes of every chunk
-    int dev = 0, sms = 152, per_sm = 1;
+    int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    per_sm = blocks_per_sm(b.order);  // kernel attributes are set up with the solver
-    if (per_sm <= 0) per_sm = std::max(1, std::min(2048 / threads, smem_sm / (int)(t->smem + 1024)));
-    const int64_t cols = (int64_t)t->grid[0] * t->grid[1] * nshot;
-    const int64_t resident = (int64_t)sms * per_sm;
-    double best = 1e300;
-    int best_c = 1;
-    for (int c = 1; c <= 64 && c <= b.ny; c++) {
-        const int64_t chunk = (b.ny + c - 1) / c;
-        const int64_t waves = (cols * c + resident - 1) / resident;
-        const double cost = (double)waves * (chunk + 2 * b.order);
-        if (cost < best - 1e-9) { best = cost; best_c = c; }
+    // y-chunking of one tile shape: balance the last wave against the 2o warm-up planes of every
+    // chunk; returns the cost in CTA-planes of the busiest slot and the chunk count
+    struct Plan { double cost; int chunks; double lanes; };
+    auto plan = [&](int sh) {
+        int tx = 0, tz = 0, hx = 0, th = 0;
+        stencil_tile_dims(b.order, sh, tx, tz, hx, th);
+        int per_sm = blocks_per_sm(b.order, sh);  // kernel attributes are set up with the solver
+        if (per_sm <= 0) per_sm = std::max(1, std::min(2048 / th, smem_sm / (int)(smem_bytes(b.order, sh) + 1024)));
+        const int64_t gx = (b.nx + tx - 1) / tx, gz = (b.nz + tz - 1) / tz;
+        const int64_t cols = gx * gz * nshot;
+        const int64_t resident = (int64_t)sms * per_sm;
+        Plan pl{1e300, 1, (double)(b.nx * b.nz) / (double)(gx * tx * gz * tz)};
+        for (int c = 1; c <= 64 && c <= b.ny; c++) {
+            const int64_t chunk = (b.ny + c - 1) / c;
+            const int64_t waves = (cols * c + resident - 1) / resident;
+            const double cost = (double)waves * (chunk + 2 * b.order);
+            if (cost < pl.cost - 1e-9) { pl.cost = cost; pl.chunks = c; }
+        }
+        return pl;
+    };
+    // tile shape: the square order-4 tile for a single shot where it costs less, counting the
+    // busiest slot's CTA-planes over the share of lanes on nodes (lanes past the box edge do the
+    // same work; measured on GB300, 64 x 16 against 32 x 32: 801^3 nodes 369.1 against 367.0
+    // Gnode-steps/s, 481^3 0.329 against 0.331 ms per step, 401^3 321.9 against 336.3, 345^3
+    // 0.145 against 0.130 ms, which this ranking orders the same way)
+    int sh = kTileDefault;
+    if (b.order == 4 && nshot == 1) {
+        if (shape == kTileSquare) {
+            sh = kTileSquare;
+        } else if (shape < 0) {
+            const Plan p0 = plan(kTileDefault), p1 = plan(kTileSquare);
+            if (p1.cost / p1.lanes < p0.cost / p0.lanes - 1e-9) sh = kTileSquare;
+        }
     }
+    t->shape = sh;
+    int threads = 256;
+    stencil_tile_dims(b.order, sh, t->tile_x, t->tile_z, t->halo_x, threads);
+    t->threads = threads;
+    t->smem = smem_bytes(b.order, sh);
+    t->grid[0] = (int)((b.nx + t->tile_x - 1) / t->tile_x);
+    t->grid[1] = (int)((b.nz + t->tile_z - 1) / t->tile_z);
+    const int best_c = plan(sh).chunks;
     t->ychunk = (int)((b.ny + best_c - 1) / best_c);
     t->grid[2] = (int)((b.ny + t->ychunk - 1) / t->ychunk);
     *out = t;

@@ -29,6 +29,7 @@ struct sem_solver {
     uint64_t mref_version = 0;
     double *d_w = nullptr;       // GLL weights (double) for the mass kernel
     semgb::StencilTables *stencil = nullptr;
+    int tile_shape = -1;  // stencil tile shape: -1 chosen per box, or a semgb::StencilTileShape
     // sponge
     bool sponge = false;
     float *d_sx = nullptr, *d_sy = nullptr, *d_sz = nullptr;

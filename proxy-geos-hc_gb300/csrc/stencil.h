@@ -32,8 +32,13 @@ struct alignas(16) ClassTable {
     float c[3][O][O][2 * O + 1][O];
 };
 
+// Tile shapes of the pass: the default for every order, and for order 4 a square 32 x 32 tile
+// that single-shot plain steps may take (the 64 x 16 default wastes more lanes on some boxes)
+enum StencilTileShape { kTileDefault = 0, kTileSquare = 1 };
+
 struct StencilTables {
     int order = 0;
+    int shape = kTileDefault;  // tile shape the kernels and the tables below are built for
     // SEM_ROUNDING_REFERENCE: the reference's assembled node-class coefficients, host memory
     // owned by the tables (null: the tensor-product operator below)
     float *class_tab = nullptr;
@@ -107,7 +112,11 @@ cudaError_t launch_group_step(const GroupMember *members, int n_members, const i
 // Tables and tiling for a box (no device buffers yet).  Returns 0 or a cudaError_t.
 // nshot > 1: the many-shot form, levels holding nshot fields one after another (traces
 // [step][receiver][shot]); dt^2/M and the sponge are shared.
-int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int nshot, StencilTables **out);
+// shape: kTileDefault, kTileSquare (order 4, one shot; otherwise the default) or -1 to choose
+int stencil_tables_create(const Box &b, const Gll &g, const Geometry &geo, int nshot, StencilTables **out,
+                          int shape = -1);
+// tile of a shape: nodes along x and z, x halo, threads per CTA
+void stencil_tile_dims(int order, int shape, int &tx, int &tz, int &hx, int &threads);
 // Describe the solver's two pressure buffers and its dt^2/M buffer with tensor maps.
 int stencil_bind(StencilTables &t, const float *p0, const float *p1, const float *a);
 // Group node-sorted receivers (device-layout indices) by owning CTA (device CSR in t).

@@ -46,7 +46,11 @@ __constant__ float c_T[kMaxOrder][kTMax];  // [order-1][l * (2o+1) + d + o]
 __constant__ float2 c_T2[kMaxOrder][kTMax];  // the same coefficients twice, for packed node pairs
 __constant__ float c_wa[kMaxOrder][kMaxOrder];  // assembled weights by local index
 
-template <int O>
+// Rows per warp instruction of the square order-4 tile (32 x 32 nodes; the default is 64 x 16),
+// which a single-shot pass can take where it wastes fewer lanes on the last x- and z-tiles.
+constexpr int kSquareRW = 4;
+
+template <int O, int RWS = SEM_STENCIL_RW>
 struct Cfg {
     // Orders 1-4 (o divides the warp count: 4 warps, 3 for o = 3): a warp's lanes split into RW
     // sets on rows o apart, and each thread owns NG row groups a further o*RW rows apart, all
@@ -60,7 +64,7 @@ struct Cfg {
     static constexpr bool SPLIT = O <= 4;
     static constexpr int NG = SPLIT ? SEM_STENCIL_NG : 1;  // row groups per thread
     static constexpr int WARPS = !SPLIT ? 5 : (O == 3 ? 3 : 8 / NG);
-    static constexpr int RW = SPLIT ? SEM_STENCIL_RW : 4;
+    static constexpr int RW = SPLIT ? RWS : 4;
     static constexpr int LANES = 32 / RW;               // lanes per row
     static constexpr int GR = O * RW;                   // rows between a thread's groups
     static constexpr int TZ = WARPS * RW * NG;          // rows per CTA
@@ -327,14 +331,14 @@ using ClassParam = typename std::conditional<REF, ClassTable<O>, NoClassTable>::
 // current level (ring: tile boxes; win: tile plus halos), the stored previous level and dt^2/M.
 // GROUP: the CTA may have more threads than the order's configuration uses (a launch that mixes
 // orders); the extra threads take part in the barriers only.
-template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF, bool GROUP>
+template <int O, bool SPONGE, int MODE, bool DIRECT, bool MULTI, bool REF, bool GROUP, int RWS = SEM_STENCIL_RW>
 __device__ __forceinline__ void stencil_cta(const CUtensorMap *rmap, const CUtensorMap *wmap, const CUtensorMap *pmap,
                                             const CUtensorMap *amap, const StencilTables &t, const StencilArgs &a,
                                             const ClassParam<O, REF> &ct, const int shot, const int bx, const int bz,
                                             const int chunk)
 {
     static_assert(!REF || DIRECT, "the reference-rounding operator is a direct form");
-    using C = Cfg<O>;
+    using C = Cfg<O, RWS>;
     constexpr int TZ = C::TZ, TX = C::TX, HX = C::HX, TXP = C::TXP, R = C::R, AUX = C::AUX;
     extern __shared__ __align__(128) unsigned char smem[];
     float *ring = reinterpret_cast<float *>(smem);

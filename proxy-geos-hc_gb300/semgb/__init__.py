@@ -22,6 +22,7 @@ SEM_OK, SEM_ERR_ARG, SEM_ERR_CUDA, SEM_ERR_OOM, SEM_ERR_TIMEOUT, SEM_ERR_UNSTABL
 KERNEL_AUTO, KERNEL_ELEMENT, KERNEL_STENCIL = 0, 1, 2
 FORM_DIRECT, FORM_DIFFERENCE = 0, 1
 ROUNDING_DEFAULT, ROUNDING_REFERENCE = 0, 1
+TILE_AUTO, TILE_DEFAULT, TILE_SQUARE = -1, 0, 1
 GROUP_ONE_LAUNCH, GROUP_BRANCHES = 0, 1
 LEVEL_CURRENT, LEVEL_PREVIOUS = 0, 1
 
@@ -64,6 +65,8 @@ _SIGS = {
     "sem_solver_set_kernel": [_VP, C.c_int],
     "sem_solver_set_operator_form": [_VP, C.c_int],
     "sem_solver_set_rounding": [_VP, C.c_int],
+    "sem_solver_set_tile_shape": [_VP, C.c_int],
+    "sem_solver_get_tile_shape": [_VP, _I32P],
     "sem_solver_set_sponge": [_VP, C.c_int, C.c_float],
     "sem_solver_set_sponge_profile": [_VP, _F32P, _F32P, _F32P],
     "sem_solver_set_sources": [_VP, C.c_int, _I64P, _F32P, C.c_int],
@@ -325,6 +328,18 @@ class Solver:
     def set_rounding(self, rounding: int):
         """ROUNDING_DEFAULT or ROUNDING_REFERENCE (the reference's float-rounded element rows)."""
         _check(lib().sem_solver_set_rounding(self._h, rounding))
+
+    def set_tile_shape(self, shape: int):
+        """TILE_AUTO (default, chosen per box), TILE_DEFAULT or TILE_SQUARE (order 4): the
+        stencil pass's tile; the same bits with every shape."""
+        _check(lib().sem_solver_set_tile_shape(self._h, shape))
+
+    @property
+    def tile_shape(self) -> int:
+        """Shape of the built stencil tables (TILE_AUTO before the first stencil step)."""
+        v = C.c_int32(0)
+        _check(lib().sem_solver_get_tile_shape(self._h, C.byref(v)))
+        return v.value
 
     def set_sponge(self, thickness: int, sigma: float):
         _check(lib().sem_solver_set_sponge(self._h, thickness, sigma))
