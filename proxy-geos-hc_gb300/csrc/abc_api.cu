@@ -50,7 +50,6 @@ struct sem_abc {
     bool face = false;
     int4 *d_tiles = nullptr;
     int64_t ntiles = 0;
-    int64_t *d_pos = nullptr;
     float *d_hist_alt = nullptr;
     int hcur = 0;
     FaceDesc faces[6];
@@ -103,7 +102,6 @@ cudaError_t enqueue_correction(sem_abc *a)
         for (int k = 0; k < 6; k++) f.face[k] = a->faces[k];
         f.tiles = a->d_tiles;
         f.ntiles = a->ntiles;
-        f.pos = a->d_pos;
         f.p_new = s->d_p[s->cur];
         f.p_cur = x.p_cur;
         f.hist = a->hist_now();
@@ -326,7 +324,6 @@ int sem_abc_destroy(sem_abc *a)
     dfree(a->d_hist);
     dfree(a->d_corr);
     dfree(a->d_tiles);
-    dfree(a->d_pos);
     dfree(a->d_hist_alt);
     delete a;
     return SEM_OK;
@@ -373,7 +370,6 @@ int sem_abc_create(sem_solver *s, sem_mlp *net, int layer_elems, sem_abc **out)
         struct Spec { int n, u, v; int64_t ulo, uhi, vlo, vhi; };
         const Spec spec[3] = {{1, 0, 2, 0, nx, 0, nz}, {2, 0, 1, 0, nx, 1, ny - 1}, {0, 2, 1, 1, nz - 1, 1, ny - 1}};
         std::vector<int4> tiles;
-        std::vector<int64_t> pos;
         for (int k = 0; k < 6; k++) {
             const Spec &sp = spec[k / 2];
             FaceDesc &f = a->faces[k];
@@ -381,27 +377,16 @@ int sem_abc_create(sem_solver *s, sem_mlp *net, int layer_elems, sem_abc **out)
             f.side = (k % 2 == 0) ? 0 : (int)(dims[sp.n] - 1);
             f.inward = (k % 2 == 0) ? 1 : -1;
             f.ulo = (int)sp.ulo; f.uhi = (int)sp.uhi; f.vlo = (int)sp.vlo; f.vhi = (int)sp.vhi;
+            // a tile row is a node of the face where it lies within [ulo, uhi) x [vlo, vhi); every
+            // such node is a boundary node (the strip of layer 0)
             for (int64_t v0 = sp.vlo; v0 < sp.vhi; v0 += kFaceTV)
-                for (int64_t u0 = sp.ulo; u0 < sp.uhi; u0 += kFaceTU) {
-                    tiles.push_back(make_int4(k, (int)u0, (int)v0, 0));
-                    for (int r = 0; r < kMlpTile; r++) {
-                        const int64_t u = u0 + r % kFaceTU, v = v0 + r / kFaceTU;
-                        if (u >= sp.uhi || v >= sp.vhi) { pos.push_back(-1); continue; }
-                        int64_t c[3];
-                        c[sp.u] = u; c[sp.v] = v; c[sp.n] = f.side;
-                        const int64_t qn = c[0] + c[2] * b.nxp + c[1] * b.nxp * b.nz;
-                        const auto it = std::lower_bound(nodes.begin(), nodes.end(), qn);
-                        pos.push_back(it != nodes.end() && *it == qn ? (int64_t)(it - nodes.begin()) : -1);
-                    }
-                }
+                for (int64_t u0 = sp.ulo; u0 < sp.uhi; u0 += kFaceTU) tiles.push_back(make_int4(k, (int)u0, (int)v0, 0));
         }
         a->face = true;
         a->ntiles = (int64_t)tiles.size();
         e = dalloc(&a->d_tiles, tiles.size());
-        if (e == cudaSuccess) e = dalloc(&a->d_pos, pos.size());
         if (e == cudaSuccess) e = dalloc(&a->d_hist_alt, (size_t)b.n_int);
         if (e == cudaSuccess) e = cudaMemcpy(a->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(a->d_pos, pos.data(), pos.size() * 8, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemset(a->d_hist_alt, 0, (size_t)b.n_int * 4);
     }
     if (e != cudaSuccess) {

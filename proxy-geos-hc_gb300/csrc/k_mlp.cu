@@ -32,15 +32,6 @@ namespace {
 #ifndef SEM_MLP_FACE_PIPE
 #define SEM_MLP_FACE_PIPE 1
 #endif
-// Epilogues of the register-resident inference forward (compile-time knob: 1 = biases entered
-// as the accumulator operand of each layer's first MMA, GELU's factor 1/2 moved into the next
-// layer's weights (W2 and w3 halved in shared memory: exact for weights of magnitude >= 2^-125),
-// layer 3 summed in packed pairs; 0 = the training forward's arithmetic: zero accumulators, bias
-// added after the products, 2-term GELU, sequential layer-3 sum).  The two round differently in
-// the last bits of the pre-activations.
-#ifndef SEM_MLP_FAST_EPI
-#define SEM_MLP_FAST_EPI 1
-#endif
 
 constexpr int H = kMlpHidden;
 constexpr int KP1 = kMlpInPad + 8;  // row stride (bf16) of X and W1
@@ -96,30 +87,11 @@ __device__ __forceinline__ float2 gelu2(float2 z)
     const float2 h = mul2(make_float2(0.5f, 0.5f), z);
     return fma2(h, t, h);
 }
-// 2 GELU(z) = z + z tanh(u): the tanh form without its factor 1/2
-__device__ __forceinline__ float2 gelu2_twice(float2 z)
-{
-    const float2 w = fma2(make_float2(kGeluCA, kGeluCA), mul2(z, z), make_float2(kGeluC, kGeluC));
-    const float2 u = mul2(z, w);
-    const float2 t = make_float2(tanh_hw(u.x), tanh_hw(u.y));
-    return fma2(z, t, z);
-}
 __device__ __forceinline__ float gelu_d(float z)
 {
     // d/dz [z/2 (1 + tanh u)] = (1 + t)/2 + z/2 (1 - t^2) (c + 3 c a z^2)
     const float t = tanh_hw(gelu_u(z));
     return fmaf(0.5f, t, 0.5f) + (0.5f * z) * fmaf(-t, t, 1.f) * fmaf(3.f * kGeluCA, z * z, kGeluC);
-}
-
-// d = a.b + (c0, c1) on both rows of the thread's fragment (one column pair, e.g. a bias)
-__device__ __forceinline__ void mma16816_c(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2], float c0,
-                                           float c1)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%10,%11,%10,%11};"
-        : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]), "f"(c0), "f"(c1));
 }
 
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
@@ -154,14 +126,7 @@ struct NetSmem {
     float b1[H], b2[H], w3[H], b3;
 };
 
-// BF16 pair halved (exact unless a value is below 2^-125 in magnitude)
-__device__ __forceinline__ uint32_t half_bf2(uint32_t x)
-{
-    return pack_bf2(__uint_as_float(x << 16) * 0.5f, __uint_as_float(x & 0xffff0000u) * 0.5f);
-}
-
-// half_out: W2 and w3 stored halved, for forward_rows_regs's epilogues
-__device__ void load_net(NetSmem &s, const MlpDev &net, bool half_out = false)
+__device__ void load_net(NetSmem &s, const MlpDev &net)
 {
     // 16-byte chunks: W1 rows are 96 bf16 (12 chunks), W2 rows 64 (8 chunks); shared rows are
     // padded to 104 and 72 elements, still 16-byte aligned
@@ -175,14 +140,12 @@ __device__ void load_net(NetSmem &s, const MlpDev &net, bool half_out = false)
 #pragma unroll 4
     for (int i = threadIdx.x; i < H * C2; i += blockDim.x) {
         const int nn = i / C2, j = i - nn * C2;
-        uint4 v = __ldg(reinterpret_cast<const uint4 *>(net.w2) + i);
-        if (half_out) v = make_uint4(half_bf2(v.x), half_bf2(v.y), half_bf2(v.z), half_bf2(v.w));
-        *reinterpret_cast<uint4 *>(s.w2 + nn * KP2 + j * 8) = v;
+        *reinterpret_cast<uint4 *>(s.w2 + nn * KP2 + j * 8) = __ldg(reinterpret_cast<const uint4 *>(net.w2) + i);
     }
     for (int i = threadIdx.x; i < H; i += blockDim.x) {
         s.b1[i] = net.b1[i];
         s.b2[i] = net.b2[i];
-        s.w3[i] = half_out ? 0.5f * net.w3[i] : net.w3[i];
+        s.w3[i] = net.w3[i];
     }
     if (threadIdx.x == 0) s.b3 = net.b3[0];
 }
@@ -292,11 +255,14 @@ __device__ void forward_rows(const NetSmem &s, const uint16_t *xs, uint16_t *h1,
 // As forward_rows for inference (no saved activations), with the hidden layer kept in registers:
 // the m16n8 accumulator fragments of layer-1 columns 16k..16k+15 (n-tiles 2k and 2k+1) are, after
 // bias, GELU and BF16 rounding, exactly the m16n8k16 A fragments of layer 2's k-step k, so no
-// shared-memory copy of the hidden activations is made.  The network's weights come from
-// load_net(.., half_out = SEM_MLP_FAST_EPI).
+// shared-memory copy of the hidden activations is made.  Same roundings and summation order as
+// forward_rows, which the training and the adjoint use: a network must be trained and
+// differentiated as it runs, and the training of the learned boundary, a feedback loop over whole
+// runs, follows last-bit differences far (biases entered as the first MMA's accumulator, which
+// round the pre-activations differently, moved the trained network's reflected energy from
+// 0.0043 to 0.011-0.045).
 __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, float (&yv)[2][2])
 {
-    constexpr bool FAST = SEM_MLP_FAST_EPI;
     const int lane = threadIdx.x & 31, q = lane & 3;
 #if SEM_MLP_LDSM
     // ldmatrix row addresses: A (rows of xs) {rows 0-7, 8-15} x {cols 0-7, 8-15}; B (rows n of
@@ -306,26 +272,13 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
 #else
     const int g = lane >> 2;
 #endif
-    // one k-step of a layer over the warp's 32 rows; the first takes the bias as its accumulator
-    auto mma_step = [&](float (&acc0)[4], float (&acc1)[4], const uint32_t (&a0)[4], const uint32_t (&a1)[4],
-                        const uint32_t (&b)[2], bool first, const float *bias, int c) {
-        if (FAST && first) {
-            const float2 bb = *reinterpret_cast<const float2 *>(bias + c);
-            mma16816_c(acc0, a0, b, bb.x, bb.y);
-            mma16816_c(acc1, a1, b, bb.x, bb.y);
-        } else {
-            mma16816(acc0, a0, b);
-            mma16816(acc1, a1, b);
-        }
-    };
     float acc[2][8][4];
-    if (!FAST)
 #pragma unroll
-        for (int mt = 0; mt < 2; mt++)
+    for (int mt = 0; mt < 2; mt++)
 #pragma unroll
-            for (int nt = 0; nt < 8; nt++)
+        for (int nt = 0; nt < 8; nt++)
 #pragma unroll
-                for (int j = 0; j < 4; j++) acc[mt][nt][j] = 0.f;
+            for (int j = 0; j < 4; j++) acc[mt][nt][j] = 0.f;
 #pragma unroll
     for (int ks = 0; ks < kMlpInPad / 16; ks++) {
         uint32_t a[2][4];
@@ -354,11 +307,12 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
             const uint32_t b[2] = {*reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0),
                                    *reinterpret_cast<const uint32_t *>(s.w1 + n * KP1 + k0 + 8)};
 #endif
-            mma_step(acc[0][nt], acc[1][nt], a[0], a[1], b, ks == 0, s.b1, nt * 8 + q * 2);
+            mma16816(acc[0][nt], a[0], b);
+            mma16816(acc[1][nt], a[1], b);
         }
     }
     // layer-1 epilogue into layer-2 A fragments: h[mt][ks] = {row g cols 16ks+2q.., row g+8 the
-    // same, row g cols 16ks+8+2q.., row g+8 the same}; FAST: 2 GELU (W2 is halved)
+    // same, row g cols 16ks+8+2q.., row g+8 the same}
     uint32_t h[2][H / 16][4];
 #pragma unroll
     for (int mt = 0; mt < 2; mt++)
@@ -367,17 +321,12 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
             const int c = nt * 8 + q * 2;
 #pragma unroll
             for (int hrow = 0; hrow < 2; hrow++) {
-                float2 z = make_float2(acc[mt][nt][hrow * 2], acc[mt][nt][hrow * 2 + 1]);
-                float2 gz;
-                if (FAST) {
-                    gz = gelu2_twice(z);
-                } else {
-                    z = add2(z, *reinterpret_cast<const float2 *>(s.b1 + c));
-                    gz = gelu2(z);
-                    acc[mt][nt][hrow * 2] = 0.f;
-                    acc[mt][nt][hrow * 2 + 1] = 0.f;
-                }
+                const float2 z = add2(make_float2(acc[mt][nt][hrow * 2], acc[mt][nt][hrow * 2 + 1]),
+                                      *reinterpret_cast<const float2 *>(s.b1 + c));
+                const float2 gz = gelu2(z);
                 h[mt][nt >> 1][(nt & 1) * 2 + hrow] = pack_bf2(gz.x, gz.y);
+                acc[mt][nt][hrow * 2] = 0.f;
+                acc[mt][nt][hrow * 2 + 1] = 0.f;
             }
         }
 #pragma unroll
@@ -395,35 +344,23 @@ __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, 
             const uint32_t b[2] = {*reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0),
                                    *reinterpret_cast<const uint32_t *>(s.w2 + n * KP2 + k0 + 8)};
 #endif
-            mma_step(acc[0][nt], acc[1][nt], h[0][ks], h[1][ks], b, ks == 0, s.b2, nt * 8 + q * 2);
+            mma16816(acc[0][nt], h[0][ks], b);
+            mma16816(acc[1][nt], h[1][ks], b);
         }
     }
 #pragma unroll
     for (int mt = 0; mt < 2; mt++)
 #pragma unroll
         for (int hrow = 0; hrow < 2; hrow++) {
-            float part;
-            if (FAST) {
-                // w3 is halved; the thread's columns summed in even/odd pairs
-                float2 pp = make_float2(0.f, 0.f);
+            float part = 0.f;
 #pragma unroll
-                for (int nt = 0; nt < 8; nt++) {
-                    const int c = nt * 8 + q * 2;
-                    const float2 gz = gelu2_twice(make_float2(acc[mt][nt][hrow * 2], acc[mt][nt][hrow * 2 + 1]));
-                    pp = fma2(*reinterpret_cast<const float2 *>(s.w3 + c), gz, pp);
-                }
-                part = pp.x + pp.y;
-            } else {
-                part = 0.f;
-#pragma unroll
-                for (int nt = 0; nt < 8; nt++) {
-                    const int c = nt * 8 + q * 2;
-                    const float2 z = add2(make_float2(acc[mt][nt][hrow * 2], acc[mt][nt][hrow * 2 + 1]),
-                                          *reinterpret_cast<const float2 *>(s.b2 + c));
-                    const float2 gz = gelu2(z);
-                    part = fmaf(s.w3[c], gz.x, part);
-                    part = fmaf(s.w3[c + 1], gz.y, part);
-                }
+            for (int nt = 0; nt < 8; nt++) {
+                const int c = nt * 8 + q * 2;
+                const float2 z = add2(make_float2(acc[mt][nt][hrow * 2], acc[mt][nt][hrow * 2 + 1]),
+                                      *reinterpret_cast<const float2 *>(s.b2 + c));
+                const float2 gz = gelu2(z);
+                part = fmaf(s.w3[c], gz.x, part);
+                part = fmaf(s.w3[c + 1], gz.y, part);
             }
             part += __shfl_xor_sync(0xffffffffu, part, 1);
             part += __shfl_xor_sync(0xffffffffu, part, 2);
@@ -707,7 +644,7 @@ __global__ void __launch_bounds__(128, 4) k_abc_correction(const MlpDev net, con
     NetSmem &s = *reinterpret_cast<NetSmem *>(smem);
     uint16_t *xs = reinterpret_cast<uint16_t *>(smem + kAbcXsOff);
     float *scale = reinterpret_cast<float *>(xs + T * KP1);
-    load_net(s, net, SEM_MLP_FAST_EPI);  // forward_rows_regs only
+    load_net(s, net);
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
     const int64_t plane = a.nxp * a.nz;
@@ -822,7 +759,7 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
     float *patch = reinterpret_cast<float *>(smem + kFacePatchOff);
     int64_t *onode = reinterpret_cast<int64_t *>(smem + kFaceOutOff);
     int *offs = reinterpret_cast<int *>(smem + kFaceOffsOff);
-    load_net(s, net, SEM_MLP_FAST_EPI);  // forward_rows_regs only
+    load_net(s, net);
     // the depth plane outside the box stays zero for every tile
     for (int i = threadIdx.x; i < 3 * kPD; i += blockDim.x) patch[(i / kPD) * kPL + i % kPD] = 0.f;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
@@ -856,9 +793,7 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
     // level 0 from the history and this kernel can write their new values in place (no tile
     // reads p^{n+1} of a boundary node, so a tile's loads may run ahead of other tiles' writes).
     // s = (sx*sz)*sy, as the step rounds it.
-    // the three sponge factors are kept apart until the store, so that no arithmetic waits on the
-    // loads before the network runs
-    float v0s[KS], v1s[KS], v2s[KS], sxs[KS], sys[KS], szs[KS];
+    float v0s[KS], v1s[KS], v2s[KS], sfs[KS];
     bool bnds[KS];
     auto load_patch = [&](int64_t tt) {
         const int4 td = a.tiles[tt];
@@ -867,7 +802,7 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
         for (int k = 0; k < KS; k++) {
             const int i = threadIdx.x + k * T;
             v0s[k] = v1s[k] = v2s[k] = 0.f;
-            sxs[k] = sys[k] = szs[k] = 1.f;
+            sfs[k] = 1.f;
             bnds[k] = false;
             if (i < NPOS) {
                 int di, vv, uu, cx, cy, cz;
@@ -879,11 +814,7 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
                     v2s[k] = a.hist[qn];
                     v1s[k] = a.p_cur[qn];
                     if (!bnds[k]) v0s[k] = a.p_new[qn];
-                    if (a.sx) {
-                        sxs[k] = __ldg(a.sx + cx);
-                        sys[k] = __ldg(a.sy + cy);
-                        szs[k] = __ldg(a.sz + cz);
-                    }
+                    if (a.sx) sfs[k] = (__ldg(a.sx + cx) * __ldg(a.sz + cz)) * __ldg(a.sy + cy);
                 }
             }
         }
@@ -904,9 +835,8 @@ __global__ void __launch_bounds__(128, 3) k_abc_face(const MlpDev net, const Abc
             if (i < NPOS) {
                 int di, vv, uu;
                 decode(f, i, di, vv, uu);
-                const float sf = (sxs[k] * szs[k]) * sys[k];
-                const float p0 = bnds[k] ? v2s[k] * sf : v0s[k];
-                const float p1 = v1s[k] * sf;  // p^n is stored without its last sponge factor
+                const float p0 = bnds[k] ? v2s[k] * sfs[k] : v0s[k];
+                const float p1 = v1s[k] * sfs[k];  // p^n is stored without its last sponge factor
                 // p^n of the tile's own nodes and their inside neighbours: the next step's
                 // p^{n-1} (every node of the two-node shell is one of these for some tile)
                 const int us = td.y - 1 + uu, vs = td.z - 1 + vv;

@@ -60,7 +60,6 @@ struct AbcFaceArgs {
     FaceDesc face[6];
     const int4 *tiles;     // (face, u0, v0, 0) per tile
     int64_t ntiles;
-    const int64_t *pos;    // [ntiles * kMlpTile]: position of each tile row in the strip (-1: none)
     float *p_new;          // p^{n+1} (sponge applied); out: the boundary nodes' new values
     const float *p_cur;    // p^n stored without its last sponge factor
     const float *hist;     // p^{n-1} (actual values) on the two-node shell, device layout
