@@ -71,8 +71,8 @@ enum { SEM_ROUNDING_DEFAULT = 0, SEM_ROUNDING_REFERENCE = 1 };
 /* Tile shape of the stencil pass (sem_solver_set_tile_shape): the nodes along x and z that one
    CTA steps.  DEFAULT: 16o x 8 for o = 1, 2 and 4 (64 x 16 at order 4), 48 x 24 at o = 3, 40 x 20
    at o = 5.  SQUARE: 32 x 32 at order 4 (other orders: the default), for the plain step of one
-   shot in the default rounding (the reference rounding, the adjoint's passes, batches and the
-   one-launch group form keep the default).  AUTO: the shape whose busiest CTA slot marches the
+   shot in the default rounding (the reference rounding, the adjoint's passes and batches keep
+   the default; a group's one launch runs each member on its own shape).  AUTO: the shape whose busiest CTA slot marches the
    fewest planes per lane on a node, from the box's node counts (on GB300, 345^3 and 401^3 nodes
    take the square tile: 0.130 against 0.145 ms and 336 against 322 Gnode-steps/s; 481^3 and
    801^3 keep the default).  Every shape gives the same bits. */

@@ -150,8 +150,8 @@ std::vector<int> group_chunks(const sem_group *g, int64_t resident)
         jobs.clear();
         for (const sem_solver *s : g->members) {
             const Box &b = s->mesh->box;
-            int tx = 0, tz = 0, hx = 0, th = 0;  // the group's tiles have the default shape
-            semgb::stencil_tile_dims(b.order, semgb::kTileDefault, tx, tz, hx, th);
+            int tx = 0, tz = 0, hx = 0, th = 0;  // the member's own tile shape
+            semgb::stencil_tile_dims(b.order, s->stencil->shape, tx, tz, hx, th);
             const int64_t cols = ((b.nx + tx - 1) / tx) * ((b.nz + tz - 1) / tz);
             const int64_t c = (b.ny + L - 1) / L, chunk = (b.ny + c - 1) / c;
             jobs.push_back({chunk + 2 * b.order, cols * c});
@@ -259,10 +259,9 @@ int build_one_launch(sem_group *g)
     if (g->ones.size() != n) g->ones.assign(n, nullptr);
     for (size_t i = 0; i < n; i++) {
         sem_solver *s = g->members[i];
-        // tables of the default tile shape (the group kernel's) over the member's levels: a
-        // member stepped alone may use another shape
+        // tables of the member's own tile shape over its levels, with the group's chunking
         StencilTables *t = nullptr;
-        if (semgb::stencil_tables_create(s->mesh->box, s->mesh->gll, s->mesh->geo, 1, &t, semgb::kTileDefault) != 0)
+        if (semgb::stencil_tables_create(s->mesh->box, s->mesh->gll, s->mesh->geo, 1, &t, s->stencil->shape) != 0)
             return sem_fail(SEM_ERR_CUDA, "stencil tables");
         g->tabs[i] = t;
         if (semgb::stencil_bind(*t, s->d_p[0], s->d_p[1], s->d_a) != 0)

@@ -10,7 +10,8 @@
 // warps) the fourth warp only takes part in the barriers.
 //
 // Members without a sponge run the sponge code with unit factors: every factor multiplies by
-// exactly 1, so the results are those of the pass without a sponge.
+// exactly 1, so the results are those of the pass without a sponge.  An order-4 member runs on
+// the tile shape of its tables (the square 32 x 32 tile where the member stepped alone takes it).
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -24,7 +25,8 @@ namespace semgb {
 namespace {
 
 static_assert(Cfg<1>::THREADS <= kGroupThreads && Cfg<2>::THREADS <= kGroupThreads &&
-                  Cfg<3>::THREADS <= kGroupThreads && Cfg<4>::THREADS <= kGroupThreads,
+                  Cfg<3>::THREADS <= kGroupThreads && Cfg<4>::THREADS <= kGroupThreads &&
+                  Cfg<4, kSquareRW>::THREADS <= kGroupThreads,
               "a group CTA holds every order's configuration");
 
 constexpr int kGroupMinBlocks = 3;
@@ -82,7 +84,13 @@ __global__ void __launch_bounds__(kGroupThreads, kGroupMinBlocks)
     case 1: stencil_cta<1, true, STENCIL_PLAIN, true, false, false, true>(rmap, wmap, pmap, amap, t, a, none, 0, bx, bz, chunk); break;
     case 2: stencil_cta<2, true, STENCIL_PLAIN, true, false, false, true>(rmap, wmap, pmap, amap, t, a, none, 0, bx, bz, chunk); break;
     case 3: stencil_cta<3, true, STENCIL_PLAIN, true, false, false, true>(rmap, wmap, pmap, amap, t, a, none, 0, bx, bz, chunk); break;
-    default: stencil_cta<4, true, STENCIL_PLAIN, true, false, false, true>(rmap, wmap, pmap, amap, t, a, none, 0, bx, bz, chunk); break;
+    default:
+        if (t.shape == kTileSquare)
+            stencil_cta<4, true, STENCIL_PLAIN, true, false, false, true, kSquareRW>(rmap, wmap, pmap, amap, t, a, none, 0,
+                                                                                     bx, bz, chunk);
+        else
+            stencil_cta<4, true, STENCIL_PLAIN, true, false, false, true>(rmap, wmap, pmap, amap, t, a, none, 0, bx, bz, chunk);
+        break;
     }
 }
 
@@ -91,7 +99,7 @@ size_t smem_upto(int max_order)
     size_t m = Cfg<1>::SMEM;
     if (max_order >= 2) m = std::max(m, Cfg<2>::SMEM);
     if (max_order >= 3) m = std::max(m, Cfg<3>::SMEM);
-    if (max_order >= 4) m = std::max(m, Cfg<4>::SMEM);
+    if (max_order >= 4) m = std::max(m, std::max(Cfg<4>::SMEM, Cfg<4, kSquareRW>::SMEM));
     return m;
 }
 

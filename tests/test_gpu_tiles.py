@@ -68,16 +68,18 @@ def test_automatic_shape_and_fallbacks(semgb_lib, cuda_device):
 
 
 def test_group_of_square_members(semgb_lib, cuda_device):
-    """Members that step alone on the square tile join a one-launch group on the default tile."""
+    """Members that step alone on the square tile keep it in a one-launch group, beside a member
+    on the default tile."""
     semgb = semgb_lib
-    dims = [(7, 7, 7), (7, 5, 6), (16, 5, 11)]
-    solo = [_solver(semgb, *d, 4, 17, 50 + i, 1, semgb.TILE_SQUARE) for i, d in enumerate(dims)]
+    dims = [(7, 7, 7), (7, 5, 6), (16, 5, 11), (9, 6, 8)]
+    shapes = [semgb.TILE_SQUARE, semgb.TILE_SQUARE, semgb.TILE_SQUARE, semgb.TILE_DEFAULT]
+    solo = [_solver(semgb, *d, 4, 17, 50 + i, 1, sh) for i, (d, sh) in enumerate(zip(dims, shapes))]
     for _, s in solo:
         s.step(17)
-    grouped = [_solver(semgb, *d, 4, 17, 50 + i, 1, semgb.TILE_SQUARE) for i, d in enumerate(dims)]
-    for _, s in grouped:
-        s.step(1)  # the members' own tables are square
-        assert s.tile_shape == semgb.TILE_SQUARE
+    grouped = [_solver(semgb, *d, 4, 17, 50 + i, 1, sh) for i, (d, sh) in enumerate(zip(dims, shapes))]
+    for (_, s), sh in zip(grouped, shapes):
+        s.step(1)  # the members' own tables
+        assert s.tile_shape == sh
     g = semgb.Group([s for _, s in grouped])
     g.step(16)
     g.synchronize()
