@@ -89,3 +89,30 @@ def test_group_of_square_members(semgb_lib, cuda_device):
         assert np.array_equal(a.traces(), b.traces())
     g.close()
     _close(*solo, *grouped)
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["direct", "difference"])
+@pytest.mark.parametrize("name", ["c2_shape_q4_12c", "q4_rand"])
+def test_square_tile_on_reference_fixtures(semgb_lib, cuda_device, name, form):
+    """The square tile on the order-4 fixtures of the compiled reference: the same bits as the
+    default tile, so the same errors against the reference and against FP64."""
+    import os
+    from test_gpu_parity import GOLDEN, rel_l2, solver_for_fixture
+    semgb = semgb_lib
+    path = [g for g in GOLDEN if os.path.basename(g) == name + ".npz"][0]
+    f = np.load(path)
+    kernel = "stencil-difference" if form else "stencil"
+    runs = []
+    for shape in (semgb.TILE_DEFAULT, semgb.TILE_SQUARE):
+        m, s = solver_for_fixture(semgb, f, kernel)
+        s.set_tile_shape(shape)
+        s.step(int(f["nsteps"]))
+        assert s.tile_shape == shape
+        runs.append((s.traces(), s.pressure(), s.pressure(semgb.LEVEL_PREVIOUS)))
+        s.close()
+        m.close()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
+    tr, p, _ = runs[1]
+    assert rel_l2(tr, f["traces"]) <= 1e-5 + 2 * rel_l2(f["traces"], f["traces64"])
+    assert rel_l2(p, f["p_cur"]) <= 1e-5 + 2 * rel_l2(f["p_cur"], f["p_cur64"])
