@@ -235,6 +235,7 @@ def run_ours(args):
     kernel = {"auto": semgb.KERNEL_AUTO, "element": semgb.KERNEL_ELEMENT,
               "stencil": semgb.KERNEL_STENCIL}[args.kernel]
     mesh, s = semgb.solver_from_workload(wl, kernel)
+    s.set_tile_shape({"auto": semgb.TILE_AUTO, "default": semgb.TILE_DEFAULT, "square": semgb.TILE_SQUARE}[args.tile])
     stream = torch.cuda.Stream()
     s.set_stream(stream.cuda_stream)
     N = mesh.n_nodes
@@ -326,7 +327,9 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded layered+perturbed velocity model)",
             "config": {"workload": wl.name, "elements": [wl.ex, wl.ey, wl.ez], "order": wl.order,
-                       "nodes": N, "kernel": resolved, "parallelism": "replicas" if ws > 1 else "single",
+                       "nodes": N, "kernel": resolved, "tile": ({0: "default", 1: "square"}.get(s.tile_shape, "n/a")
+                                                                if resolved == "stencil" else "n/a"),
+                       "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (2 GB per field), no flush"},
             "roofline": roof,
             **extra,
@@ -790,6 +793,8 @@ def main():
                          "and --impl reference")
     ap.add_argument("--cpu-steps", type=int, default=6, help="cpu_baseline steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tile", choices=["auto", "default", "square"], default="auto",
+                    help="tile shape of the stencil pass (auto: chosen per box; square: order 4 only)")
     ap.add_argument("--no-rows", action="store_true", help="skip the element-path / batched / uneven / adjoint / learned-boundary rows")
     ap.add_argument("--case", choices=["batch40", "abc86", "q5_80", "uneven_small"], default=None,
                     help="run a small fixed case for a kernel profile instead of the benchmark")
