@@ -646,7 +646,8 @@ def measure_learned(steps_time: int = 40):
     best round kept, then steepest descent on the reflected energy of whole runs with the
     gradient from the adjoint of the time loop) against the same sponge alone and a 20-element
     sponge, reflected energy against a padded run, for the training source and for a source
-    position not used in training, after the sample rounds and after the adjoint training.
+    position not used in training, after the sample rounds and after the adjoint training; and
+    the trained network on a region twice as large (12^3 elements, twice the run length).
     Speed at the 120^3 size: 120^3 Q4 with a 20-element sponge (region of interest 80^3)
     against 86^3 Q4 with a 3-element sponge and the network, ms per step of each time loop
     (CUDA events)."""
@@ -680,6 +681,17 @@ def measure_learned(steps_time: int = 40):
     e_thick_g, _ = LB.reflected_energy(thick_gentle, None)
     e_net_h, _ = LB.reflected_energy(thin_h, net)
     e_thin_h, _ = LB.reflected_energy(thin_h, None)
+    # the same network on a region twice as large (12^3 elements; run length and padding scaled
+    # with it, the padded run's own boundary still too far to reflect back in time): how the
+    # trained boundary carries over to a larger model than it was trained on
+    big = dict(common, interior=12, steps=520)
+    thin_b = LB.Setup(sponge_t=3, pad=24, layer=0, sigma=thin_sigma, **big)
+    thick_b = LB.Setup(sponge_t=20, pad=24, layer=0, **big)
+    t0 = time.perf_counter()
+    e_net_b, _ = LB.reflected_energy(thin_b, net)
+    e_thin_b, _ = LB.reflected_energy(thin_b, None)
+    e_thick_b, _ = LB.reflected_energy(thick_b, None)
+    t_big = time.perf_counter() - t0
     # speed at size
     stream = torch.cuda.Stream()
     out = {}
@@ -711,6 +723,9 @@ def measure_learned(steps_time: int = 40):
                                             "reflected_energy_sponge3": e_thin_h,
                                             "reflected_energy_network_samples_only": e_sup_h},
                         "reflected_energy_network_samples_only": e_sup,
+                        "region_12c": {"steps": big["steps"], "reflected_energy_network_sponge3": e_net_b,
+                                       "reflected_energy_sponge3": e_thin_b, "reflected_energy_sponge20": e_thick_b,
+                                       "seconds": t_big},
                         "training": log, "training_seconds": t_train,
                         "adjoint_training": {"loss_per_iteration": adj_hist, "seconds": t_adj,
                                              "method": "steepest descent, line search along the adjoint gradient"}},
