@@ -728,7 +728,7 @@ def measure_learned(steps_time: int = 40):
                                        "seconds": t_big},
                         "training": log, "training_seconds": t_train,
                         "adjoint_training": {"loss_per_iteration": adj_hist, "seconds": t_adj,
-                                             "method": "steepest descent, line search along the adjoint gradient"}},
+                                             "method": "steepest descent, line searches along the adjoint gradient and along its sign scaled by each parameter"}},
             "speed": out,
             "speedup_per_step": out["sponge20_120c"]["ms_per_step"] / out["net_sponge3_86c"]["ms_per_step"]}
 

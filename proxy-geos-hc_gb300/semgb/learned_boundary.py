@@ -198,7 +198,7 @@ def train_network(s: Setup, net: Mlp, rounds: int = 3, epochs: int = 12, per_ste
 
 
 def train_through_adjoint(s, net: Mlp, iters: int = 20, step: float = 0.01, lr: float = 1e-3,
-                          method: str = "line", keep_best: bool = True):
+                          method: str = "line+relative", keep_best: bool = True):
     """Trains the network on the reflected energy itself, through the adjoint of the whole time
     loop.  `s` is one Setup or a list of Setups (e.g. several source positions around the same
     region of interest: the loss is then the mean of theirs).  Every evaluation runs T with the
@@ -212,6 +212,11 @@ def train_through_adjoint(s, net: Mlp, iters: int = 20, step: float = 0.01, lr: 
     step * 2^k, k = -2..2, the best kept; `step` follows the accepted one, quartered when none
     lowers the loss and reset when it has shrunk a thousandfold): a 260-step rollout makes the
     loss rough, and a search along the exact gradient never accepts a step that raises it.
+    method "line+relative": the same search, and beside it one along -sign(g) scaled by each
+    parameter's magnitude (relative steps 2^-9 .. 2^-3): the BF16 weight matrices keep 8
+    significant bits, so steps along the normalised gradient small enough to lower a rough loss
+    often change no weight at all, while a relative step moves every weight whose gradient is
+    not zero; the lower of the two searches is taken.
     method "adam": one Adam step of rate `lr` per gradient.  With keep_best the parameters of
     the lowest loss seen are kept.  Returns the loss after every iteration (entry 0: before
     training)."""
@@ -267,7 +272,17 @@ def train_through_adjoint(s, net: Mlp, iters: int = 20, step: float = 0.01, lr: 
         d = (d / nrm).astype(np.float32)
         tried = [(loss_at(theta + step * (2.0 ** k) * d), k) for k in (-2, -1, 0, 1, 2)]
         lk, k = min(tried)
-        if lk < e:
+        lr_best, cand = np.inf, None
+        if method == "line+relative":
+            rel = (-np.sign(g) * np.maximum(np.abs(theta.astype(np.float64)), 1e-3)).astype(np.float32)
+            for j in (9, 7, 5, 3):
+                th = theta + np.float32(2.0 ** -j) * rel
+                lj = loss_at(th)
+                if lj < lr_best:
+                    lr_best, cand = lj, th
+        if lr_best < min(lk, e):
+            theta = cand
+        elif lk < e:
             theta = theta + step * (2.0 ** k) * d
             step *= 2.0 ** k
         else:
