@@ -197,6 +197,39 @@ def train_network(s: Setup, net: Mlp, rounds: int = 3, epochs: int = 12, per_ste
     return log
 
 
+def descent_step(theta, g, e: float, step: float, step0: float, loss_at, method: str = "line+relative"):
+    """One iteration of train_through_adjoint's searches from parameters theta (FP32) with loss e
+    and gradient g: returns (theta, step, ok), ok False when the gradient is zero or not finite.
+    loss_at(p) evaluates the loss at parameters p.  The gradient search tries step * 2^k along the
+    normalised negative gradient (k = -2..2); "line+relative" also tries -sign(g) * max(|theta|,
+    1e-3) * 2^-j (j = 9, 7, 5, 3).  The lowest loss below e is taken (the relative search on a
+    tie); `step` follows an accepted gradient step, is quartered when neither search lowers the
+    loss, and is reset to step0 once it has shrunk a thousandfold."""
+    d = -g
+    nrm = float(np.linalg.norm(d))
+    if not np.isfinite(nrm) or nrm == 0.0:
+        return theta, step, False
+    d = (d / nrm).astype(np.float32)
+    tried = [(loss_at(theta + step * (2.0 ** k) * d), k) for k in (-2, -1, 0, 1, 2)]
+    lk, k = min(tried)
+    lr_best, cand = np.inf, None
+    if method == "line+relative":
+        rel = (-np.sign(g) * np.maximum(np.abs(theta.astype(np.float64)), 1e-3)).astype(np.float32)
+        for j in (9, 7, 5, 3):
+            th = theta + np.float32(2.0 ** -j) * rel
+            lj = loss_at(th)
+            if lj < lr_best:
+                lr_best, cand = lj, th
+    if lr_best < min(lk, e):
+        return cand, step, True
+    if lk < e:
+        return theta + step * (2.0 ** k) * d, step * 2.0 ** k, True
+    step *= 0.25
+    if step < step0 * 1e-3:
+        step = step0  # no progress at any step length: search again from the start
+    return theta, step, True
+
+
 def train_through_adjoint(s, net: Mlp, iters: int = 20, step: float = 0.01, lr: float = 1e-3,
                           method: str = "line+relative", keep_best: bool = True):
     """Trains the network on the reflected energy itself, through the adjoint of the whole time
@@ -265,30 +298,9 @@ def train_through_adjoint(s, net: Mlp, iters: int = 20, step: float = 0.01, lr: 
             net.adam_step(g.astype(np.float32), lr)
             theta = net.params.copy()
             continue
-        d = -g
-        nrm = float(np.linalg.norm(d))
-        if not np.isfinite(nrm) or nrm == 0.0:
+        theta, step, ok = descent_step(theta, g, e, step, step0, loss_at, method)
+        if not ok:
             break
-        d = (d / nrm).astype(np.float32)
-        tried = [(loss_at(theta + step * (2.0 ** k) * d), k) for k in (-2, -1, 0, 1, 2)]
-        lk, k = min(tried)
-        lr_best, cand = np.inf, None
-        if method == "line+relative":
-            rel = (-np.sign(g) * np.maximum(np.abs(theta.astype(np.float64)), 1e-3)).astype(np.float32)
-            for j in (9, 7, 5, 3):
-                th = theta + np.float32(2.0 ** -j) * rel
-                lj = loss_at(th)
-                if lj < lr_best:
-                    lr_best, cand = lj, th
-        if lr_best < min(lk, e):
-            theta = cand
-        elif lk < e:
-            theta = theta + step * (2.0 ** k) * d
-            step *= 2.0 ** k
-        else:
-            step *= 0.25
-            if step < step0 * 1e-3:
-                step = step0  # no progress at any step length: search again from the start
     net.params = best[1] if keep_best else theta
     for *_, objs in runs:
         for o in objs:
