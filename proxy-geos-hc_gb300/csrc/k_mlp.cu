@@ -259,8 +259,8 @@ __device__ void forward_rows(const NetSmem &s, const uint16_t *xs, uint16_t *h1,
 // forward_rows, which the training and the adjoint use: a network must be trained and
 // differentiated as it runs, and the training of the learned boundary, a feedback loop over whole
 // runs, follows last-bit differences far (biases entered as the first MMA's accumulator, which
-// round the pre-activations differently, moved the trained network's reflected energy from
-// 0.0043 to 0.011-0.045).
+// round the pre-activations differently, moved the reflected energy of the network trained with
+// the gradient line search from 0.0043 to 0.011-0.045).
 __device__ void forward_rows_regs(const NetSmem &s, const uint16_t *xs, int wr, float (&yv)[2][2])
 {
     const int lane = threadIdx.x & 31, q = lane & 3;
