@@ -94,6 +94,14 @@ public:
     sem_solver *handle() const { return h_; }
     void setKernel(int k) { check(sem_solver_set_kernel(h_, k), "sem_solver_set_kernel"); }
     void setOperatorForm(int f) { check(sem_solver_set_operator_form(h_, f), "sem_solver_set_operator_form"); }
+    void setRounding(int r) { check(sem_solver_set_rounding(h_, r), "sem_solver_set_rounding"); }
+    void setTileShape(int shape) { check(sem_solver_set_tile_shape(h_, shape), "sem_solver_set_tile_shape"); }
+    int tileShape() const
+    {
+        int shape = SEM_TILE_AUTO;
+        check(sem_solver_get_tile_shape(h_, &shape), "sem_solver_get_tile_shape");
+        return shape;
+    }
     void setSponge(int thickness, float sigma) { check(sem_solver_set_sponge(h_, thickness, sigma), "sem_solver_set_sponge"); }
     void setSources(const std::vector<int64_t> &elements, const std::vector<float> &wavelet, int nsamples)
     {
